@@ -1,0 +1,379 @@
+"""Benchmark of the GB300 N-body step.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+A step is one pass of the hot path over one galaxy: Barnes-Hut (octree keys,
+radix sort, topology, mass pass, traversal, kick-drift) or direct sum (force
+kernel + kick-drift).  `value` is body-steps/s with the particle state
+resident in HBM; `e2e` is the same metric through the reference-facing C-ABI
+(nb_init_particles from pinned host records, nb_step, nb_write_back into the
+records) with the host<->device copies inside the timed region.
+
+Workloads (seeded synthetic galaxies; no dataset is involved):
+  bh1m        Barnes-Hut, N=1,048,576 exponential disk (90%) + Hernquist bulge
+              (10%), theta=0.5, eps=0.005, dt=5e-4              [default]
+  direct262k  direct sum, N=262,144, two Plummer spheres on a parabolic orbit,
+              eps=0.01, dt=1e-3
+  direct4096  direct sum, N=4096 Plummer sphere, eps=0.01, dt=1e-3
+
+--impl reference times the reference's CPU algorithm (the oracle's
+restatement of BruteForceCPU / BarnesHut on all host cores) on the same
+workload, a bounded sample per step.
+Multi-GPU: the step does not shard across GPUs in this build; --gpus N runs N
+independent replicas (one galaxy per rank, different seeds) and reports the
+aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "procedural-universe_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOADS = {
+    "bh1m": dict(kind=2, n=1 << 20, model="disk", eps=0.005, dt=5e-4, theta=0.5,
+                 desc="Barnes-Hut, N=1,048,576 disk (rd=1, z0=0.1, 5% dispersion) + 10% Hernquist bulge (a=0.2), "
+                      "theta=0.5, eps=0.005, dt=5e-4"),
+    "direct262k": dict(kind=0, n=262144, model="collision", eps=0.01, dt=1e-3, theta=0.5,
+                       desc="direct sum, N=262,144, two Plummer spheres (a=1, M=1 each) on a parabolic orbit "
+                            "10 apart (pericentre 1), eps=0.01, dt=1e-3"),
+    "direct4096": dict(kind=0, n=4096, model="plummer", eps=0.01, dt=1e-3, theta=0.5,
+                       desc="direct sum, N=4096 Plummer sphere (a=1, M=1), eps=0.01, dt=1e-3"),
+}
+METRIC = "body-steps/s"
+L2_FLUSH_BYTES = 512 << 20       # > 129 MB L2
+FLOP_PER_INTERACTION = 20
+
+
+def seed_workload(w, seed):
+    import nbody_gb300 as nb
+    if w["model"] == "disk":
+        return nb.seed_disk(seed, w["n"])
+    if w["model"] == "collision":
+        return nb.seed_collision(seed, w["n"])
+    return nb.seed_plummer(seed, w["n"])
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+        self._thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self._proc = None
+            return
+        self._thread = threading.Thread(target=self._read, daemon=True)
+        self._thread.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self) -> dict:
+        if self._proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self._proc.terminate()
+        try:
+            self._proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self._proc.kill()
+        if self._thread:
+            self._thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if s[3 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the reference's CPU algorithm (oracle restatement), bounded.
+# --------------------------------------------------------------------------
+def cpu_baseline(w, pm, v, budget_s=12.0):
+    from oracle import oracle as O
+    threads = O.default_threads()
+    cores = threads + 1                 # workers + the calling thread (CThreadPool layout)
+    rec = O.particles_from_soa(pm, v)
+    n = w["n"]
+    S = w["eps"] ** 2
+    rng = np.random.default_rng(0)
+    if w["kind"] == 2:
+        t0 = time.perf_counter()
+        tree = O.OracleTree(rec)
+        t_build = time.perf_counter() - t0
+        m = 4096
+        while True:
+            targets = np.sort(rng.choice(n, m, replace=False))
+            t0 = time.perf_counter()
+            tree.forces_subset(targets, G=1.0, S=S, theta=w["theta"])
+            t_walk = time.perf_counter() - t0
+            if t_walk > 2.0 or m >= n:
+                break
+            m = min(n, m * 4)
+        tree.close()
+        step_s = t_build + t_walk * n / m
+        sample = ("serial octree build of all %d bodies (%.2f s) + traversal of %d sampled bodies on %d threads "
+                  "(%.2f s), extrapolated to one step of %d bodies" % (n, t_build, m, threads, t_walk, n))
+    else:
+        m = min(n, 1024)
+        while True:
+            targets = np.sort(rng.choice(n, m, replace=False))
+            t0 = time.perf_counter()
+            O.direct_forces_subset(rec, targets, G=1.0, S=S)
+            t_f = time.perf_counter() - t0
+            if t_f > min(2.0, budget_s) or m >= n:
+                break
+            m = min(n, m * 4)
+        step_s = t_f * n / m
+        sample = ("direct-sum forces of %d sampled target bodies against all %d sources on %d threads (%.2f s), "
+                  "extrapolated to one step of %d bodies" % (m, n, threads, t_f, n))
+    return {"value": n / step_s, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample,
+            "step_s": step_s}
+
+
+def run_reference(args, w):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    pm, v = seed_workload(w, 1234)
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(w, pm, v)
+        if i >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    val = float(np.median(vals)) if vals else 0.0
+    out = {"metric": METRIC, "value": val, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w["n"] / val if val else None,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+           "data": "synthetic (seeded)", "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"]},
+           "cpu_baseline": {"value": val, "unit": METRIC, "cores": base["cores"] if base else None,
+                            "kind": "port", "sample": base["sample"] if base else ""},
+           "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+# --------------------------------------------------------------------------
+def run_ours(args, w):
+    import torch
+    import nbody_gb300 as nb
+
+    world, rank, local = dist_env()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n = w["n"]
+    pm, v = seed_workload(w, 1234 + rank)
+    stream = torch.cuda.Stream(device=dev)
+    sim = nb.NBodySim(kind=w["kind"], device=dev, softening2=w["eps"] ** 2, theta=w["theta"],
+                      stream=stream.cuda_stream)
+    rec_host = nb.records_from_soa(pm, v)
+    sim.init(rec_host)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    dt = w["dt"]
+
+    # warm-up (untimed)
+    for _ in range(args.warmup):
+        sim.step(dt, 1)
+    sim.synchronize()
+
+    # ---- device-resident timed region ----
+    lib = nb.lib()
+    launches0 = ctypes.c_uint64(0)
+    lib.nb_launch_count(sim.handle, ctypes.byref(launches0))
+    lib.nb_profile_enable(sim.handle, 1)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    inter_total = 0
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()                       # L2 flush between timed steps (untimed)
+            evs[k][0].record(stream)
+            sim.step(dt, 1)
+            evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(step_ms))
+    inter_last = sim.last_interactions()
+    launches1 = ctypes.c_uint64(0)
+    lib.nb_launch_count(sim.handle, ctypes.byref(launches1))
+    phases = {}
+    names = ["direct_force", "direct_update", "keys", "sort", "topology", "mass", "traverse", "update"]
+    for ph, nm in enumerate(names):
+        ms = ctypes.c_double(0)
+        cnt = ctypes.c_uint64(0)
+        lib.nb_profile_read(sim.handle, ph, ctypes.byref(ms), ctypes.byref(cnt))
+        if cnt.value:
+            phases[nm] = {"ms_total": ms.value, "launches": int(cnt.value), "ms_avg": ms.value / cnt.value}
+    lib.nb_profile_enable(sim.handle, 0)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms * 1e-3)
+
+    # ---- roofline of the dominant kernel ----
+    peaks, peak_src = measured_peaks()
+    if w["kind"] == 2:
+        dom = "traverse"
+        ph = phases.get(dom, {})
+        # algorithmic bytes per launch: body record read (16 B) + acceleration write (16 B) per body, plus one
+        # 16-B node/body record per interaction
+        alg_bytes = 32.0 * n + 16.0 * inter_last
+        achieved = alg_bytes / (ph.get("ms_avg", float("nan")) * 1e-3) / 1e9
+        roof = {"kernel": "k_traverse", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                "peak_source": peak_src + " hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes}
+    else:
+        dom = "direct_force"
+        ph = phases.get(dom, {})
+        fp32 = ctypes.c_double(0)
+        lib.nb_probe_fp32_peak(dev, ctypes.byref(fp32))
+        flops = FLOP_PER_INTERACTION * float(inter_last)
+        achieved = flops / (ph.get("ms_avg", float("nan")) * 1e-3) / 1e12
+        roof = {"kernel": "k_direct_force", "bound": "fp32", "achieved": achieved, "peak": fp32.value,
+                "unit": "TFLOP/s", "frac": achieved / fp32.value if fp32.value else None, "traffic": None,
+                "peak_source": "measured on this GPU by an FMA-chain probe (nb_probe_fp32_peak)",
+                "flops_per_launch": flops, "interactions_per_launch": float(inter_last)}
+
+    # ---- end-to-end through the C-ABI with pinned host records ----
+    e2e = None
+    if not args.no_e2e:
+        nbytes = n * nb.PARTICLE_DTYPE.itemsize
+        pinned = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        buf = (ctypes.c_char * nbytes).from_address(pinned.data_ptr())
+        host = np.frombuffer(buf, dtype=nb.PARTICLE_DTYPE, count=n)
+        host[:] = rec_host
+        e2e_steps = max(1, min(args.steps, 5))
+        sim.init(host)
+        sim.step(dt, 1)
+        sim.write_back(host)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.init(host)            # H2D of this step's inputs (104-B records)
+            sim.step(dt, 1)
+            sim.write_back(host)      # D2H of the result into the records
+        torch.cuda.synchronize()
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": world * n * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": n * 104,
+               "d2h_bytes_per_step": n * 64, "steps": e2e_steps}
+
+    # ---- force error vs the FP64 oracle on the GPU (sampled targets) ----
+    rng = np.random.default_rng(1)
+    targets = np.sort(rng.choice(n, min(n, 4096), replace=False)).astype(np.int32)
+    F = sim.compute_forces()
+    F64 = sim.fp64_forces(targets)
+    ferr = float(np.linalg.norm(F[targets] - F64) / np.linalg.norm(F64))
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, pm, v)
+        cpu.pop("step_s", None)
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (Kahan-compensated) + f64 diagnostics",
+        "data": "synthetic (seeded galaxies)",
+        "config": {"workload": args.workload, "desc": w["desc"], "n": n, "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "flushed (512 MB write) before every timed step"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(launches1.value - launches0.value),
+        "clocks": clk,
+        "interactions_per_step": inter_last,
+        "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)),
+        "phases_ms_avg": {k: v_["ms_avg"] for k, v_ in phases.items()},
+        "wall_s_timed_region": t_wall,
+    }
+    print(json.dumps(out))
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="direct262k", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    import nb_build
+    nb_build.build()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_ours(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

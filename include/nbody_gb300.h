@@ -1,0 +1,213 @@
+/*
+ * nbody_gb300.h -- C-ABI of the GB300 N-body step.
+ *
+ * This is the drop-in boundary for the simulator interface of
+ * Procedural-Universe (src/Sim/INBodySim.hpp:19-25):
+ *
+ *     class INBodySim {
+ *         virtual void Init(std::vector<Particle>& particles) = 0;
+ *         virtual void Update(float dt) = 0;
+ *         virtual void RenderDebug(Matrix view, Matrix proj) {}
+ *     };
+ *     std::unique_ptr<INBodySim> CreateNBodySim(ID3D11DeviceContext*, ENBodySim);
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (NB_OK or a negative NB_E* code). No C++ exception crosses the boundary.
+ * A handle's calls must be serialised by the caller (the reference calls its
+ * simulator from one thread only); different handles may be used from
+ * different threads.  All compute runs as CUDA kernels on one GPU; there is
+ * no CPU fallback: on a machine without a usable GPU nb_create fails with
+ * NB_ECUDA.
+ *
+ * include/cuda_nbody_sim.hpp wraps these calls in a C++ class with the
+ * reference's Init/Update shape.
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NB_OK         0
+#define NB_EINVAL    -1   /* bad argument (null pointer, size, NaN/inf input, bad params) */
+#define NB_ENOMEM    -2   /* device or host allocation failed / over the memory budget   */
+#define NB_ECUDA     -3   /* a CUDA runtime call failed (message in nb_last_error)      */
+#define NB_ETIMEOUT  -4   /* a bounded device-side wait ran out; the step was abandoned */
+#define NB_EBADSTATE -5   /* call out of order (e.g. nb_step before nb_init_*)           */
+#define NB_ENOTSUP   -6   /* combination of options not supported                        */
+
+/* ---- simulator kinds: mirrors ENBodySim (src/Sim/INBodySim.hpp:11-17) ---- */
+#define NB_SIM_BRUTE_FORCE   0   /* BruteForceCPU (src/Sim/BruteForceCPU.cpp)            */
+#define NB_SIM_BRUTE_FORCE_GPU 1 /* BruteForceGPU: same direct sum, same kernels as 0    */
+#define NB_SIM_BARNES_HUT    2   /* BarnesHut + Octree (src/Sim/BarnesHut.cpp, Octree.cpp) */
+
+/* ---- force laws ---------------------------------------------------------- */
+/* Reference law, Phys::Gravity (src/Sim/Physics.hpp:25-35):
+ *     F_i = sum_j -G m_i m_j / (|p_i-p_j|^2 + S) * normalize(p_i - p_j)
+ * with S = softening2.  Plummer law: F_i = sum_j G m_i m_j (p_j-p_i) / (r^2+S)^{3/2}. */
+#define NB_LAW_REFERENCE 0
+#define NB_LAW_PLUMMER   1
+
+/* Reference record, struct Particle (src/Render/Misc/Particle.hpp:8-18):
+ * 104 bytes, Position float3 @0, Colour float4 @12, OriginalColour float4 @28,
+ * 4 bytes padding @44, Velocity double3 @48, Forces double3 @72, Mass double @96.
+ * This is also the record of the .nbody file format. */
+typedef struct nb_particle {
+    float  position[3];
+    float  colour[4];
+    float  original_colour[4];
+    float  _pad;
+    double velocity[3];
+    double forces[3];
+    double mass;
+} nb_particle;
+
+/* Light-weight render record, LWParticle (src/Render/Misc/Particle.hpp:20-25). */
+typedef struct nb_render_vertex {
+    float position[3];
+    float colour[4];
+    float scale;
+} nb_render_vertex;
+
+/* Parameters. Fields default (nb_default_params) to the values of the
+ * reference configuration translated to N-body units:
+ *   G          Phys::G            (src/Sim/Physics.hpp:9)      default 1
+ *   softening2 Phys::S            (src/Sim/Physics.hpp:10)     default 1e-4 (eps = 0.01)
+ *   theta      Octree::Theta      (src/Sim/Octree.cpp:5)       default 0.5
+ *   pos_scale  Phys::StarSystemScale divisor of the drift (src/Sim/BruteForceCPU.cpp:66) default 1
+ *   bounds_half half-width of the Barnes-Hut root cube (src/Sim/BarnesHut.cpp:14-21) default 4000
+ *   max_depth  octree depth cap (the reference has none; 21 = 63-bit keys)
+ *   leaf_size  bodies per leaf before a split (reference: 1)                                */
+typedef struct nb_params {
+    int    kind;          /* NB_SIM_* */
+    int    law;           /* NB_LAW_* */
+    double G;
+    double softening2;
+    double theta;
+    double pos_scale;
+    float  bounds_half;
+    int    max_depth;     /* 1..21 */
+    int    leaf_size;     /* >= 1 */
+    int    device;        /* CUDA device ordinal */
+    void*  stream;        /* cudaStream_t to launch on, or NULL for a library-owned stream */
+    int    flags;         /* NB_FLAG_* */
+} nb_params;
+
+#define NB_FLAG_NONE            0
+#define NB_FLAG_NO_COMPENSATION 1  /* plain FP32 accumulation and update (for error studies) */
+
+/* FP64 diagnostics: energy, linear momentum, angular momentum (all FP64
+ * reductions on the GPU). The potential is the one of the selected law:
+ * reference law phi(r) = -(G mi mj / eps)(pi/2 - atan(r/eps)); Plummer
+ * phi(r) = -G mi mj / sqrt(r^2 + eps^2). */
+typedef struct nb_diag {
+    double kinetic;
+    double potential;
+    double total;
+    double momentum[3];
+    double angular_momentum[3];
+    double mass;
+    double centre_of_mass[3];
+} nb_diag;
+
+typedef struct nb_sim nb_sim;
+
+int  nb_default_params(nb_params* params);
+
+/* CreateNBodySim (src/Sim/INBodySim.cpp:7-27). */
+int  nb_create(const nb_params* params, nb_sim** out);
+int  nb_destroy(nb_sim* sim);
+const char* nb_last_error(const nb_sim* sim);   /* message of the last failed call, "" if none */
+const char* nb_sim_name(int kind);              /* NBodySimGetName (src/Sim/INBodySim.cpp:29-39) */
+
+/* INBodySim::Init (src/Sim/BruteForceCPU.cpp:20-23, src/Sim/BarnesHut.cpp:39-42,
+ * src/Sim/BruteForceGPU.cpp:38-43): uploads n reference records. Masses are
+ * rounded to float on the device (exact for float-representable masses, which
+ * every seeder in this library produces). May be called again with another n. */
+int  nb_init_particles(nb_sim* sim, const nb_particle* particles, size_t n);
+/* Same from structure-of-arrays host buffers: pos_mass = n x (x,y,z,m),
+ * vel = n x (vx,vy,vz,unused). */
+int  nb_init_soa(nb_sim* sim, const float* pos_mass4, const float* vel4, size_t n);
+size_t nb_count(const nb_sim* sim);
+
+/* INBodySim::Update(dt) (src/Sim/BruteForceCPU.cpp:45-74, src/Sim/BarnesHut.cpp:44-96):
+ * nsteps kick-drift steps of size dt, asynchronous on the handle's stream
+ * (nb_synchronize waits; reads below synchronise). */
+int  nb_step(nb_sim* sim, float dt, int nsteps);
+int  nb_synchronize(nb_sim* sim);
+
+/* Writes Position, Velocity and Forces back into n reference records, as
+ * Update leaves them: Forces are zero after a direct-sum step
+ * (src/Sim/BruteForceCPU.cpp:72) and hold the last Barnes-Hut force otherwise
+ * (src/Sim/BarnesHut.cpp:81-95). Colour, OriginalColour and Mass are untouched. */
+int  nb_write_back(nb_sim* sim, nb_particle* particles, size_t n);
+
+/* Host copies of the state. Any pointer may be NULL. force3 is the force
+ * (m * acceleration) of the last force evaluation. */
+int  nb_read_state(nb_sim* sim, float* pos3, double* vel3, double* force3);
+/* Evaluates forces at the current positions without stepping and returns
+ * them (n x 3 doubles, force on each body). */
+int  nb_compute_forces(nb_sim* sim, double* force3);
+/* Interactions evaluated by the last force evaluation (pairwise + monopole). */
+int  nb_last_interactions(nb_sim* sim, uint64_t* interactions);
+
+/* FP64 direct-sum oracle on the GPU for m sampled target bodies against all n
+ * sources, with the handle's law, G and softening (force on each target). */
+int  nb_fp64_forces(nb_sim* sim, const int32_t* targets, size_t m, double* force3);
+/* half_kick_dt != 0: velocities are synchronised to the positions first,
+ * v + a(x) * half_kick_dt (pass dt/2 after kick-drift steps of size dt). */
+int  nb_diagnostics(nb_sim* sim, float half_kick_dt, nb_diag* out);
+
+/* Stream the handle launches on (cudaStream_t). */
+void* nb_stream(nb_sim* sim);
+
+/* ---- measurement ---------------------------------------------------------- */
+/* Per-phase GPU time measured with CUDA events recorded on the handle's
+ * stream around each phase's kernels (enable before the region to measure). */
+#define NB_PHASE_DIRECT_FORCE   0   /* K1 direct-sum force kernel                    */
+#define NB_PHASE_DIRECT_UPDATE  1   /* K7 partial fold + kick-drift                  */
+#define NB_PHASE_KEYS           2   /* K2 Morton keys                                */
+#define NB_PHASE_SORT           3   /* K3 radix sort                                 */
+#define NB_PHASE_TOPOLOGY       4   /* K4 octree topology                            */
+#define NB_PHASE_MASS           5   /* K5 bottom-up mass / centre of mass            */
+#define NB_PHASE_TRAVERSE       6   /* K6 tree traversal                             */
+#define NB_PHASE_UPDATE         7   /* kick-drift after a tree force pass            */
+#define NB_PHASE_COUNT          10
+int  nb_profile_enable(nb_sim* sim, int on);      /* on != 0 clears the totals */
+/* Total milliseconds and launches of a phase since enabling (synchronises). */
+int  nb_profile_read(nb_sim* sim, int phase, double* total_ms, uint64_t* launches);
+/* Kernel launches issued by this handle since creation. */
+int  nb_launch_count(nb_sim* sim, uint64_t* launches);
+/* Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA) from
+ * a dependent-chain FMA kernel filling every SM, timed with CUDA events. */
+int  nb_probe_fp32_peak(int device, double* tflops);
+
+/* Headless render hand-off: fills n render vertices (LWParticle) with the
+ * current positions and the given per-body colour (n x float4) and scale. */
+int  nb_render_vertices(nb_sim* sim, const float* colour4, float scale, nb_render_vertex* out, size_t n);
+
+/* ---- initial conditions (seeders) ---------------------------------------- */
+/* Counter-based seeded generators. Output: n x (x,y,z,m) and n x (vx,vy,vz,0),
+ * host buffers. Every mass is float-representable. */
+int  nb_seed_plummer(uint64_t seed, size_t n, double total_mass, double a,
+                     float* pos_mass4, float* vel4);
+/* Exponential disk (scale length rd, sech^2 height z0, mass fraction
+ * 1-bulge_frac) plus Hernquist bulge (scale ab), circular velocities with a
+ * Gaussian dispersion of `dispersion` times the circular speed. */
+int  nb_seed_disk(uint64_t seed, size_t n, double total_mass, double rd, double z0,
+                  double bulge_frac, double ab, double dispersion,
+                  float* pos_mass4, float* vel4);
+/* Two equal Plummer spheres (each mass total_mass/2, scale a) on a parabolic
+ * orbit with pericentre `pericentre`, starting `separation` apart, in the
+ * centre-of-mass frame. */
+int  nb_seed_collision(uint64_t seed, size_t n, double a, double separation,
+                       double pericentre, float* pos_mass4, float* vel4);
+#ifdef __cplusplus
+}
+#endif
+#endif /* NBODY_GB300_H */

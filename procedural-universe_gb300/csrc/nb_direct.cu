@@ -1,0 +1,338 @@
+// nb_direct.cu -- direct-sum gravity (K1) and the compensated kick-drift (K7).
+//
+// Replaces BruteForceCPU::Exec/Update (src/Sim/BruteForceCPU.cpp:25-74) and
+// the D3D11 pair BruteForceGPU + shaders/Compute/Gravity.csh, Update.csh
+// (src/Sim/BruteForceGPU.cpp:45-71).
+//
+// Layout: bodies are float4 (x, y, z, m) in HBM, padded to a multiple of
+// kPad with zero-mass bodies.  A work unit of K1 is (target block, source
+// range): BLOCK*IPT target bodies held in registers against a contiguous
+// range of source tiles.  Each 128-body source tile (2 KB) is moved from HBM
+// to shared memory by the TMA engine (cp.async.bulk) into a double buffer
+// guarded by mbarriers; every thread then reads each source body as a
+// broadcast float4.  Forces are accumulated in FP32 in groups of kFold
+// sources, and each group sum is folded into a Kahan-compensated total.
+// Each unit writes its (sum, compensation) partials; K7 folds the partials of
+// all source ranges in a fixed order (deterministic), applies G, and performs
+// the kick-drift with Kahan-compensated velocity and position.
+//
+// Force law per source j on target i (reference law, Phys::Gravity,
+// src/Sim/Physics.hpp:25-35, S = softening2):
+//     a_i += m_j (p_j - p_i) / (r (r^2 + S)),   r = |p_j - p_i|
+// evaluated with one MUFU.RSQ: 1/(r (r^2+S)) = rsqrt(r^2 (r^2+S)^2 + tiny).
+// tiny = 1e-30 keeps the self pair (r = 0, dp = 0) finite, so it adds
+// exactly zero; it is below the rounding of every real pair with S >= 1e-12.
+// Plummer law: a_i += m_j (p_j - p_i) (r^2 + S)^{-3/2}.
+#include "nb_common.cuh"
+#include "nb_internal.hpp"
+#include <algorithm>
+
+namespace nb {
+
+constexpr int kFold = 32;            // sources summed in plain FP32 before a Kahan fold
+constexpr float kTiny = 1e-30f;
+
+template <int LAW>
+__device__ __forceinline__ void interact(const float4 pj, float xi, float yi, float zi, float S, float& ax,
+                                         float& ay, float& az) {
+    float dx = pj.x - xi;
+    float dy = pj.y - yi;
+    float dz = pj.z - zi;
+    if (LAW == NB_LAW_REFERENCE) {
+        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        float s = r2 + S;
+        float t = fmaf(r2 * s, s, kTiny);
+        float w = pj.w * rsqrt_approx(t);
+        ax = fmaf(w, dx, ax);
+        ay = fmaf(w, dy, ay);
+        az = fmaf(w, dz, az);
+    } else {
+        float q = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, S)));
+        float inv = rsqrt_approx(q);
+        float w = pj.w * inv * (inv * inv);
+        ax = fmaf(w, dx, ax);
+        ay = fmaf(w, dy, ay);
+        az = fmaf(w, dz, az);
+    }
+}
+
+// K1: grid (target blocks, source ranges). Writes part[split][i] (sum) and
+// part[splits + split][i] (compensation).
+template <int LAW, int BLOCK, int IPT, bool COMP>
+__global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict__ pos, int n_pad,
+                                                        int tiles_per_split, int ntiles, int splits, float S,
+                                                        float4* __restrict__ part, int* __restrict__ err) {
+    __shared__ __align__(128) float4 tile[2][kTileJ];
+    __shared__ __align__(8) uint64_t bar[2];
+
+    const int split = blockIdx.y;
+    const int ibase = blockIdx.x * BLOCK * IPT + threadIdx.x;
+
+    float xi[IPT], yi[IPT], zi[IPT];
+    float sx[IPT], sy[IPT], sz[IPT], cx[IPT], cy[IPT], cz[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        float4 p = pos[ibase + k * BLOCK];
+        xi[k] = p.x; yi[k] = p.y; zi[k] = p.z;
+        sx[k] = sy[k] = sz[k] = 0.f;
+        cx[k] = cy[k] = cz[k] = 0.f;
+    }
+
+    const int t_begin = split * tiles_per_split;
+    const int nt = max(0, min(ntiles, t_begin + tiles_per_split) - t_begin);
+    constexpr uint32_t kBytes = kTileJ * sizeof(float4);
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 2 && q < nt; ++q) {
+            mbar_arrive_expect_tx(&bar[q], kBytes);
+            bulk_g2s(tile[q], pos + (size_t)(t_begin + q) * kTileJ, kBytes, &bar[q]);
+        }
+    }
+
+    int t = 0;
+    bool abandoned = false;
+    for (; t < nt; ++t) {
+        const int b = t & 1;
+        const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((t >> 1) & 1));
+        const float4* tj = tile[b];
+#pragma unroll 1
+        for (int f = 0; f < kTileJ; f += kFold) {
+            float tx[IPT], ty[IPT], tz[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) tx[k] = ty[k] = tz[k] = 0.f;
+#pragma unroll 4
+            for (int j = 0; j < kFold; ++j) {
+                const float4 pj = tj[f + j];
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) interact<LAW>(pj, xi[k], yi[k], zi[k], S, tx[k], ty[k], tz[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                if (COMP) {
+                    kahan_add(sx[k], cx[k], tx[k]);
+                    kahan_add(sy[k], cy[k], ty[k]);
+                    kahan_add(sz[k], cz[k], tz[k]);
+                } else {
+                    sx[k] += tx[k]; sy[k] += ty[k]; sz[k] += tz[k];
+                }
+            }
+        }
+        // Every thread is done with tile[b]; agree on the wait outcome.
+        if (__syncthreads_or(!ok)) { abandoned = true; break; }
+        if (threadIdx.x == 0 && t + 2 < nt) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[b], kBytes);
+            bulk_g2s(tile[b], pos + (size_t)(t_begin + t + 2) * kTileJ, kBytes, &bar[b]);
+        }
+    }
+    if (abandoned) {
+        // Let the copies still in flight land before the block's shared
+        // memory is released (bounded), then report.
+        if (threadIdx.x == 0) {
+            for (int q = t; q < nt && q < t + 2; ++q) (void)mbar_wait_bounded(&bar[q & 1], (uint32_t)((q >> 1) & 1));
+            record_error(err, DEV_WAIT_TIMEOUT);
+        }
+        return;
+    }
+    float4* psum = part + (size_t)split * n_pad;
+    float4* pcmp = part + (size_t)(splits + split) * n_pad;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int i = ibase + k * BLOCK;
+        psum[i] = make_float4(sx[k], sy[k], sz[k], 0.f);
+        pcmp[i] = make_float4(cx[k], cy[k], cz[k], 0.f);
+    }
+}
+
+// K7: fold the partials of all source ranges (fixed order), apply G, add the
+// pending initial forces, store the acceleration and, when update != 0,
+// kick-drift: v += a dt; x += v dt / scale, both Kahan-compensated
+// (src/Sim/BruteForceCPU.cpp:61-73).
+__global__ void k_direct_reduce_update(const float4* __restrict__ part, int splits, int n, int n_pad, float G,
+                                       const float4* __restrict__ finit, float4* __restrict__ acc,
+                                       float4* __restrict__ pos, float4* __restrict__ posc,
+                                       float4* __restrict__ vel, float4* __restrict__ velc, float dt,
+                                       float inv_scale, int update, int comp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+    for (int s = 0; s < splits; ++s) {
+        const float4 p = part[(size_t)s * n_pad + i];
+        const float4 c = part[(size_t)(splits + s) * n_pad + i];
+        kahan_add(ax, kx, p.x);
+        kahan_add(ay, ky, p.y);
+        kahan_add(az, kz, p.z);
+        qx += c.x; qy += c.y; qz += c.z;
+    }
+    float3 a = make_float3(G * (ax - (kx + qx)), G * (ay - (ky + qy)), G * (az - (kz + qz)));
+    if (finit) {
+        const float4 f = finit[i];
+        a.x += f.x; a.y += f.y; a.z += f.z;
+    }
+    acc[i] = make_float4(a.x, a.y, a.z, 0.f);
+    if (!update) return;
+    float4 v = vel[i], vc = velc[i], x = pos[i], xc = posc[i];
+    if (comp) {
+        kahan_add(v.x, vc.x, a.x * dt);
+        kahan_add(v.y, vc.y, a.y * dt);
+        kahan_add(v.z, vc.z, a.z * dt);
+        kahan_add(x.x, xc.x, ((v.x - vc.x) * dt) * inv_scale);
+        kahan_add(x.y, xc.y, ((v.y - vc.y) * dt) * inv_scale);
+        kahan_add(x.z, xc.z, ((v.z - vc.z) * dt) * inv_scale);
+        velc[i] = vc;
+        posc[i] = xc;
+    } else {
+        v.x += a.x * dt; v.y += a.y * dt; v.z += a.z * dt;
+        x.x += (v.x * dt) * inv_scale; x.y += (v.y * dt) * inv_scale; x.z += (v.z * dt) * inv_scale;
+    }
+    vel[i] = v;
+    pos[i] = x;
+}
+
+// Kick-drift from a stored acceleration (Barnes-Hut path,
+// src/Sim/BarnesHut.cpp:81-95).
+__global__ void k_kick_drift(const float4* __restrict__ acc, int n, float4* __restrict__ pos,
+                             float4* __restrict__ posc, float4* __restrict__ vel, float4* __restrict__ velc,
+                             float dt, float inv_scale, int comp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = acc[i];
+    float4 v = vel[i], vc = velc[i], x = pos[i], xc = posc[i];
+    if (comp) {
+        kahan_add(v.x, vc.x, a.x * dt);
+        kahan_add(v.y, vc.y, a.y * dt);
+        kahan_add(v.z, vc.z, a.z * dt);
+        kahan_add(x.x, xc.x, ((v.x - vc.x) * dt) * inv_scale);
+        kahan_add(x.y, xc.y, ((v.y - vc.y) * dt) * inv_scale);
+        kahan_add(x.z, xc.z, ((v.z - vc.z) * dt) * inv_scale);
+        velc[i] = vc;
+        posc[i] = xc;
+    } else {
+        v.x += a.x * dt; v.y += a.y * dt; v.z += a.z * dt;
+        x.x += (v.x * dt) * inv_scale; x.y += (v.y * dt) * inv_scale; x.z += (v.z * dt) * inv_scale;
+    }
+    vel[i] = v;
+    pos[i] = x;
+}
+
+namespace {
+
+template <int LAW, int BLOCK, int IPT, bool COMP>
+void launch_force_t(dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps, int ntiles, int splits,
+                    float S, float4* part, int* err) {
+    k_direct_force<LAW, BLOCK, IPT, COMP><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S, part, err);
+}
+
+template <int LAW, bool COMP>
+bool launch_force_law(int block, int ipt, dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps,
+                      int ntiles, int splits, float S, float4* part, int* err) {
+#define NB_CASE(B, I)                                                                      \
+    if (block == B && ipt == I) {                                                          \
+        launch_force_t<LAW, B, I, COMP>(grid, st, pos, n_pad, tps, ntiles, splits, S, part, err); \
+        return true;                                                                       \
+    }
+    NB_CASE(64, 1) NB_CASE(64, 2) NB_CASE(64, 4) NB_CASE(64, 8)
+    NB_CASE(128, 1) NB_CASE(128, 2) NB_CASE(128, 4) NB_CASE(128, 8)
+    NB_CASE(256, 1) NB_CASE(256, 2) NB_CASE(256, 4)
+#undef NB_CASE
+    return false;
+}
+
+}  // namespace
+
+int direct_splits(const nb_sim* sim, const DirectTuning& t, size_t n_pad) {
+    const int ntiles = (int)(n_pad / kTileJ);
+    const int iblocks = (int)(n_pad / (size_t)(t.block * t.ipt));
+    int splits = t.splits;
+    if (splits <= 0) {
+        const int target = std::max(1, sim->sm_count) * 24;   // many short units: dynamic balance
+        splits = (target + iblocks - 1) / iblocks;
+        // keep the partials (2 float4 per body per split) within 512 MB
+        const size_t cap = (512ull << 20) / (n_pad * 2 * sizeof(float4));
+        splits = (int)std::min<size_t>((size_t)splits, std::max<size_t>(1, cap));
+    }
+    splits = std::max(1, std::min(splits, ntiles));
+    const int tps = (ntiles + splits - 1) / splits;
+    return (ntiles + tps - 1) / tps;
+}
+
+size_t direct_part_entries(const nb_sim* sim, const DirectTuning& t, size_t n_pad) {
+    return (size_t)direct_splits(sim, t, n_pad) * 2 * n_pad;
+}
+
+static DirectTuning default_tuning(size_t n_pad) {
+    DirectTuning t;
+    t.block = 128;
+    t.ipt = n_pad >= 65536 ? 4 : (n_pad >= 16384 ? 2 : 1);
+    return t;
+}
+
+cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
+    DirectTuning t = sim->tune;
+    if (t.block <= 0 || t.ipt <= 0) t = default_tuning(sim->n_pad);
+    // A tuning whose target block does not divide the padded size falls back.
+    if (sim->n_pad % (size_t)(t.block * t.ipt) != 0) t = default_tuning(sim->n_pad);
+    const int splits = direct_splits(sim, t, sim->n_pad);
+    const size_t need = (size_t)splits * 2 * sim->n_pad;
+    if (need > sim->part_cap) {
+        if (sim->part) cudaFree(sim->part);
+        sim->part = nullptr;
+        sim->part_cap = 0;
+        cudaError_t e = cudaMalloc(&sim->part, need * sizeof(float4));
+        if (e != cudaSuccess) return e;
+        sim->part_cap = need;
+    }
+    const int ntiles = (int)(sim->n_pad / kTileJ);
+    const int tps = (ntiles + splits - 1) / splits;
+    dim3 grid((unsigned)(sim->n_pad / (size_t)(t.block * t.ipt)), (unsigned)splits);
+    const float S = (float)sim->prm.softening2;
+    const bool comp = !(sim->prm.flags & NB_FLAG_NO_COMPENSATION);
+    bool ok;
+    {
+    PhaseScope ps(sim, 0);
+    if (sim->prm.law == NB_LAW_PLUMMER)
+        ok = comp ? launch_force_law<NB_LAW_PLUMMER, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
+                                                          (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
+                                                          sim->d_err)
+                  : launch_force_law<NB_LAW_PLUMMER, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
+                                                           (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
+                                                           sim->d_err);
+    else
+        ok = comp ? launch_force_law<NB_LAW_REFERENCE, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
+                                                            (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
+                                                            sim->d_err)
+                  : launch_force_law<NB_LAW_REFERENCE, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
+                                                             (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
+                                                             sim->d_err);
+    }
+    if (!ok) return cudaErrorInvalidConfiguration;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int n = (int)sim->n;
+    const float inv_scale = (float)(1.0 / sim->prm.pos_scale);
+    PhaseScope ps(sim, 1);
+    k_direct_reduce_update<<<(n + 255) / 256, 256, 0, sim->stream>>>(
+        sim->part, splits, n, (int)sim->n_pad, (float)sim->prm.G, sim->finit_pending ? sim->finit : nullptr,
+        sim->acc, sim->pos, sim->posc, sim->vel, sim->velc, dt, inv_scale, update ? 1 : 0, comp ? 1 : 0);
+    sim->finit_pending = false;
+    const double nn = (double)sim->n;
+    sim->inter_last = (uint64_t)(nn * (nn - 1.0));
+    return cudaGetLastError();
+}
+
+cudaError_t kick_drift(nb_sim* sim, float dt) {
+    const int n = (int)sim->n;
+    const bool comp = !(sim->prm.flags & NB_FLAG_NO_COMPENSATION);
+    PhaseScope ps(sim, 7);
+    k_kick_drift<<<(n + 255) / 256, 256, 0, sim->stream>>>(sim->acc, n, sim->pos, sim->posc, sim->vel, sim->velc,
+                                                           dt, (float)(1.0 / sim->prm.pos_scale), comp ? 1 : 0);
+    return cudaGetLastError();
+}
+
+}  // namespace nb

@@ -1,0 +1,297 @@
+"""ctypes binding of libnbody_gb300.so (the C-ABI in include/nbody_gb300.h).
+
+This module is the binding a Python caller (tests, bench) uses; it adds no
+compute of its own.  ``NBodySim`` mirrors the reference simulator interface
+INBodySim (src/Sim/INBodySim.hpp:19-25): ``init(particles)`` and
+``update(dt)`` on a caller-owned array of 104-byte Particle records.
+
+The library must exist (built by build.py); there is no fallback: loading
+fails loudly when it is missing, and every GPU call raises ``NBodyError``
+with the library's message when the CUDA path cannot run.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
+
+NB_OK, NB_EINVAL, NB_ENOMEM, NB_ECUDA, NB_ETIMEOUT, NB_EBADSTATE, NB_ENOTSUP = 0, -1, -2, -3, -4, -5, -6
+SIM_BRUTE_FORCE, SIM_BRUTE_FORCE_GPU, SIM_BARNES_HUT = 0, 1, 2
+LAW_REFERENCE, LAW_PLUMMER = 0, 1
+FLAG_NONE, FLAG_NO_COMPENSATION = 0, 1
+
+PARTICLE_DTYPE = np.dtype(
+    [
+        ("position", "<f4", (3,)),
+        ("colour", "<f4", (4,)),
+        ("original_colour", "<f4", (4,)),
+        ("_pad", "<f4"),
+        ("velocity", "<f8", (3,)),
+        ("forces", "<f8", (3,)),
+        ("mass", "<f8"),
+    ]
+)
+assert PARTICLE_DTYPE.itemsize == 104
+
+RENDER_DTYPE = np.dtype([("position", "<f4", (3,)), ("colour", "<f4", (4,)), ("scale", "<f4")])
+
+TREE_NODE_DTYPE = np.dtype(
+    [
+        ("level", "<i4"),
+        ("count", "<i4"),
+        ("first_child", "<i4"),
+        ("body", "<i4"),
+        ("prefix", "<u8"),
+        ("mass", "<f8"),
+        ("com", "<f4", (3,)),
+        ("side", "<f4"),
+        ("lo", "<f4", (3,)),
+        ("bucket_begin", "<i4"),
+        ("bucket_end", "<i4"),
+    ]
+)
+
+
+class nb_params(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("law", ctypes.c_int),
+        ("G", ctypes.c_double),
+        ("softening2", ctypes.c_double),
+        ("theta", ctypes.c_double),
+        ("pos_scale", ctypes.c_double),
+        ("bounds_half", ctypes.c_float),
+        ("max_depth", ctypes.c_int),
+        ("leaf_size", ctypes.c_int),
+        ("device", ctypes.c_int),
+        ("stream", ctypes.c_void_p),
+        ("flags", ctypes.c_int),
+    ]
+
+
+class nb_diag(ctypes.Structure):
+    _fields_ = [
+        ("kinetic", ctypes.c_double),
+        ("potential", ctypes.c_double),
+        ("total", ctypes.c_double),
+        ("momentum", ctypes.c_double * 3),
+        ("angular_momentum", ctypes.c_double * 3),
+        ("mass", ctypes.c_double),
+        ("centre_of_mass", ctypes.c_double * 3),
+    ]
+
+
+class NBodyError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("nbody error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads the in-tree library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libnbody_gb300.so is missing (run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, sz, i32, f32, f64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_float, ctypes.c_double
+        sig = {
+            "nb_default_params": ([vp], i32),
+            "nb_create": ([vp, vp], i32),
+            "nb_destroy": ([vp], i32),
+            "nb_last_error": ([vp], ctypes.c_char_p),
+            "nb_sim_name": ([i32], ctypes.c_char_p),
+            "nb_init_particles": ([vp, vp, sz], i32),
+            "nb_init_soa": ([vp, vp, vp, sz], i32),
+            "nb_count": ([vp], sz),
+            "nb_step": ([vp, f32, i32], i32),
+            "nb_synchronize": ([vp], i32),
+            "nb_write_back": ([vp, vp, sz], i32),
+            "nb_read_state": ([vp, vp, vp, vp], i32),
+            "nb_compute_forces": ([vp, vp], i32),
+            "nb_last_interactions": ([vp, vp], i32),
+            "nb_fp64_forces": ([vp, vp, sz, vp], i32),
+            "nb_diagnostics": ([vp, f32, vp], i32),
+            "nb_stream": ([vp], vp),
+            "nb_render_vertices": ([vp, vp, f32, vp, sz], i32),
+            "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
+            "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
+            "nb_seed_collision": ([ctypes.c_uint64, sz, f64, f64, f64, vp, vp], i32),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_params(**kw) -> nb_params:
+    p = nb_params()
+    lib().nb_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if k == "stream":
+            v = ctypes.c_void_p(v) if v else None
+        setattr(p, k, v)
+    return p
+
+
+# ---- seeders (host C++ in the library; no GPU needed) ----------------------
+
+def seed_plummer(seed: int, n: int, total_mass=1.0, a=1.0):
+    pm = np.zeros((n, 4), np.float32)
+    v = np.zeros((n, 4), np.float32)
+    rc = lib().nb_seed_plummer(seed, n, total_mass, a, _ptr(pm), _ptr(v))
+    if rc:
+        raise NBodyError(rc, "nb_seed_plummer")
+    return pm, v
+
+
+def seed_disk(seed: int, n: int, total_mass=1.0, rd=1.0, z0=0.1, bulge_frac=0.1, ab=0.2, dispersion=0.05):
+    pm = np.zeros((n, 4), np.float32)
+    v = np.zeros((n, 4), np.float32)
+    rc = lib().nb_seed_disk(seed, n, total_mass, rd, z0, bulge_frac, ab, dispersion, _ptr(pm), _ptr(v))
+    if rc:
+        raise NBodyError(rc, "nb_seed_disk")
+    return pm, v
+
+
+def seed_collision(seed: int, n: int, a=1.0, separation=10.0, pericentre=1.0):
+    pm = np.zeros((n, 4), np.float32)
+    v = np.zeros((n, 4), np.float32)
+    rc = lib().nb_seed_collision(seed, n, a, separation, pericentre, _ptr(pm), _ptr(v))
+    if rc:
+        raise NBodyError(rc, "nb_seed_collision")
+    return pm, v
+
+
+def records_from_soa(pos_mass: np.ndarray, vel: np.ndarray | None = None) -> np.ndarray:
+    n = pos_mass.shape[0]
+    p = np.zeros(n, dtype=PARTICLE_DTYPE)
+    p["position"] = pos_mass[:, :3]
+    p["mass"] = pos_mass[:, 3].astype(np.float64)
+    if vel is not None:
+        p["velocity"] = vel[:, :3].astype(np.float64)
+    p["colour"] = 1.0
+    p["original_colour"] = 1.0
+    return p
+
+
+class NBodySim:
+    """One simulator handle (nb_sim*), shaped like INBodySim."""
+
+    def __init__(self, kind=SIM_BARNES_HUT, **params):
+        self._h = ctypes.c_void_p()
+        self.params = default_params(kind=kind, **params)
+        rc = lib().nb_create(ctypes.byref(self.params), ctypes.byref(self._h))
+        if rc:
+            raise NBodyError(rc, "nb_create failed (no usable CUDA device?)")
+        self.n = 0
+
+    # -- plumbing --
+    def _check(self, rc: int, what: str):
+        if rc:
+            msg = lib().nb_last_error(self._h)
+            raise NBodyError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if self._h:
+            lib().nb_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return lib().nb_stream(self._h) or 0
+
+    # -- INBodySim --
+    def init(self, particles: np.ndarray):
+        """INBodySim::Init: uploads the caller's 104-byte records."""
+        p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+        self._check(lib().nb_init_particles(self._h, _ptr(p), p.shape[0]), "nb_init_particles")
+        self.n = p.shape[0]
+
+    def init_soa(self, pos_mass: np.ndarray, vel: np.ndarray):
+        pm = np.ascontiguousarray(pos_mass, np.float32)
+        v = np.ascontiguousarray(vel, np.float32)
+        assert pm.shape == v.shape and pm.shape[1] == 4
+        self._check(lib().nb_init_soa(self._h, _ptr(pm), _ptr(v), pm.shape[0]), "nb_init_soa")
+        self.n = pm.shape[0]
+
+    def step(self, dt: float, nsteps: int = 1):
+        self._check(lib().nb_step(self._h, dt, nsteps), "nb_step")
+
+    def update(self, dt: float, particles: np.ndarray | None = None):
+        """INBodySim::Update: one step, then the records are updated in place."""
+        self.step(dt, 1)
+        if particles is not None:
+            self.write_back(particles)
+
+    def synchronize(self):
+        self._check(lib().nb_synchronize(self._h), "nb_synchronize")
+
+    def write_back(self, particles: np.ndarray):
+        assert particles.dtype == PARTICLE_DTYPE and particles.flags.c_contiguous
+        self._check(lib().nb_write_back(self._h, _ptr(particles), particles.shape[0]), "nb_write_back")
+
+    def read_state(self):
+        pos = np.zeros((self.n, 3), np.float32)
+        vel = np.zeros((self.n, 3), np.float64)
+        force = np.zeros((self.n, 3), np.float64)
+        self._check(lib().nb_read_state(self._h, _ptr(pos), _ptr(vel), _ptr(force)), "nb_read_state")
+        return pos, vel, force
+
+    def compute_forces(self) -> np.ndarray:
+        f = np.zeros((self.n, 3), np.float64)
+        self._check(lib().nb_compute_forces(self._h, _ptr(f)), "nb_compute_forces")
+        return f
+
+    def last_interactions(self) -> int:
+        v = ctypes.c_uint64(0)
+        self._check(lib().nb_last_interactions(self._h, ctypes.byref(v)), "nb_last_interactions")
+        return int(v.value)
+
+    def fp64_forces(self, targets: np.ndarray) -> np.ndarray:
+        t = np.ascontiguousarray(targets, np.int32)
+        out = np.zeros((t.shape[0], 3), np.float64)
+        self._check(lib().nb_fp64_forces(self._h, _ptr(t), t.shape[0], _ptr(out)), "nb_fp64_forces")
+        return out
+
+    def diagnostics(self, half_kick_dt: float = 0.0) -> dict:
+        d = nb_diag()
+        self._check(lib().nb_diagnostics(self._h, half_kick_dt, ctypes.byref(d)), "nb_diagnostics")
+        return dict(kinetic=d.kinetic, potential=d.potential, total=d.total, momentum=np.array(d.momentum[:]),
+                    angular_momentum=np.array(d.angular_momentum[:]), mass=d.mass,
+                    centre_of_mass=np.array(d.centre_of_mass[:]))
+
+    def render_vertices(self, colour: np.ndarray | None = None, scale: float = 1.0) -> np.ndarray:
+        out = np.zeros(self.n, RENDER_DTYPE)
+        c = None if colour is None else np.ascontiguousarray(colour, np.float32)
+        self._check(lib().nb_render_vertices(self._h, _ptr(c), scale, _ptr(out), self.n), "nb_render_vertices")
+        return out
