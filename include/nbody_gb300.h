@@ -166,6 +166,41 @@ int  nb_diagnostics(nb_sim* sim, float half_kick_dt, nb_diag* out);
 /* Stream the handle launches on (cudaStream_t). */
 void* nb_stream(nb_sim* sim);
 
+/* ---- Barnes-Hut octree export (Octree, src/Sim/Octree.cpp:16-145) ------- */
+/* Morton keys: the concatenated 3-bit octant path a body takes from the root
+ * in Octree::Add, octant = x + 2y + 4z (src/Sim/Octree.cpp:25-41), max_depth
+ * levels, the first level in the most significant bits.  depth[i] = levels
+ * descended (max_depth for a body in the tree; 0 and key ~0 for a body outside
+ * the root cube, which the reference drops but counts).  Keys are those of
+ * the current positions. */
+int  nb_tree_keys(nb_sim* sim, uint64_t* keys, int32_t* depth);
+/* Nodes of the tree of the current positions.  Every non-empty node is one
+ * record; the non-empty children of an internal node are consecutive records
+ * in octant order starting at first_child (the reference also creates the
+ * empty siblings, which hold no body and no mass).  Record 0 is the root. */
+typedef struct nb_tree_node {
+    int32_t level;        /* 0 = root */
+    int32_t count;        /* NumParticles: bodies in the subtree                */
+    int32_t first_child;  /* record of the first non-empty child, -1 for a leaf */
+    int32_t body;         /* body index of a one-body leaf, else -1             */
+    uint64_t prefix;      /* octant path of the node (3*level bits)              */
+    double  mass;         /* TotalMass                                           */
+    float   com[3];       /* CentreOfMass                                        */
+    float   side;         /* Bounds.BottomRight.x - Bounds.TopLeft.x             */
+    float   lo[3];        /* Bounds.TopLeft                                      */
+    int32_t bucket_begin; /* leaf at the depth cap holding > 1 body: its range  */
+    int32_t bucket_end;   /* in nb_tree_order's sorted order, else -1           */
+} nb_tree_node;
+int  nb_tree_size(nb_sim* sim, size_t* nodes);
+int  nb_tree_nodes(nb_sim* sim, nb_tree_node* nodes, size_t capacity);
+int  nb_tree_order(nb_sim* sim, int32_t* order);   /* body index at each sorted position */
+/* stats8: bodies in the root cube, internal nodes, node records, bodies whose
+ * path met a gap between float child bounds (keys and topology are exact
+ * when this is 0), depth-cap buckets whose bodies differ (the reference would
+ * split them further), failed internal lookups (always 0), bodies outside
+ * the root cube, 0. */
+int  nb_tree_stats(nb_sim* sim, int64_t* stats8);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* Per-phase GPU time measured with CUDA events recorded on the handle's
  * stream around each phase's kernels (enable before the region to measure). */

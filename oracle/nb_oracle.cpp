@@ -371,6 +371,9 @@ struct Tree {
                 key = (key << 3) | (uint64_t)oct;
                 ++depth;
             }
+            /* a path cut short by a gap between float child bounds keeps its
+             * octants left-aligned (the lower levels read as octant 0) */
+            if (depth < max_depth) key <<= 3 * (max_depth - depth);
             keys[b] = key; body_depth[b] = depth;
         }
     }

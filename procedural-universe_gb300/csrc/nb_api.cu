@@ -192,6 +192,7 @@ int force_pass(nb_sim* s, float dt, bool update) {
         if (e != cudaSuccess) return cuda_fail(s, e, "direct_force_update");
     }
     s->forces_fresh = !update;
+    if (update) s->tree_valid = false;
     return NB_OK;
 }
 

@@ -26,36 +26,69 @@ struct DirectTuning {
 };
 
 // Device arrays of a Barnes-Hut octree (structure of arrays).
+//
+// Bodies are sorted by their octant path (key); the tree keeps every
+// non-empty node as a "cell".  Cell 0 is the root; the non-empty children of
+// an internal node occupy consecutive cells in octant order.
 struct TreeBuffers {
-    size_t node_cap = 0;        // capacity in cells
-    size_t body_cap = 0;
-    // per body (sorted order and keys)
-    uint64_t* keys = nullptr;      // octant path (63 bits) per body, input order
-    uint64_t* keys_alt = nullptr;  // radix sort ping-pong
-    int32_t* order = nullptr;      // body index at each sorted position
-    int32_t* order_alt = nullptr;
-    int32_t* depth = nullptr;      // levels descended per body (input order)
-    uint8_t* delta = nullptr;      // common levels of sorted neighbours i, i+1
-    int32_t* own_scan = nullptr;   // per sorted position: internal nodes it opens (scanned)
-    int32_t* close_pos = nullptr;  // scratch for range ends
-    // per cell (internal + leaf cells), cell 0 = root
-    float4* cell_com = nullptr;    // (com.x, com.y, com.z, float(mass))
-    double* cell_mass = nullptr;   // TotalMass
-    int32_t* cell_child = nullptr; // internal: first child cell; leaf: -1
-    int32_t* cell_count = nullptr; // bodies in the subtree
-    int32_t* cell_first = nullptr; // first sorted position of the subtree
-    float4* cell_lo = nullptr;     // (TopLeft.xyz, side)
-    int32_t* cell_level = nullptr;
-    uint64_t* cell_prefix = nullptr;
-    int32_t* cell_parent = nullptr;
-    int32_t* cell_pending = nullptr;  // bottom-up arrival counters
-    int32_t* counters = nullptr;      // [0] cells used, [1] internal nodes, [2] max level, ...
-    // radix sort scratch
-    uint32_t* hist = nullptr;      // per-block digit histograms
-    size_t hist_cap = 0;
-    int32_t* sort_state = nullptr; // device-side pass control
-    // traversal output
+    size_t body_cap = 0;   // sort capacity (multiple of the sort tile)
+    size_t int_cap = 0;    // internal nodes
+    size_t cell_cap = 0;   // cells
+    size_t hash_cap = 0;   // power of two
+    size_t scan_cap = 0;   // scan block-sum entries
+    size_t hist_cap = 0;   // radix histogram entries
+    // per body
+    uint64_t* keys[2] = {nullptr, nullptr};  // radix ping-pong (input order in [0] before the sort)
+    int32_t* vals[2] = {nullptr, nullptr};   // original index per sorted position
+    int32_t* depth = nullptr;                // levels descended (input order)
+    float4* spos = nullptr;                  // positions in sorted order
+    int32_t* pos_nint = nullptr;             // internal nodes starting at a position (scanned in place)
+    int32_t* leaf_level = nullptr;           // level of the leaf starting at a position, -1 if none
+    int32_t* leaf_count = nullptr;           // bodies of that leaf
+    int32_t* leaf_parent = nullptr;          // internal node holding that leaf
+    // per internal node (numbered by first body, then level)
+    int32_t* int_level = nullptr;
+    int32_t* int_first = nullptr;
+    int32_t* int_parent = nullptr;
+    uint32_t* int_mask = nullptr;            // non-empty child octants
+    int32_t* int_nint = nullptr;             // internal children
+    int32_t* int_pending = nullptr;          // bottom-up arrivals
+    int32_t* int_block = nullptr;            // first child cell
+    int32_t* int_cell = nullptr;             // own cell
+    uint64_t* int_code = nullptr;            // (1 << 3 level) | prefix
+    // per cell
+    float4* cell_com = nullptr;              // (centre of mass, float(TotalMass))
+    int4* cell_meta = nullptr;               // (first child cell | first sorted body, count, side bits, kind | nchild << 4)
+    double* cell_mass = nullptr;             // TotalMass
+    float4* cell_lo = nullptr;               // (TopLeft.xyz, side)
+    float4* cell_hi = nullptr;               // (BottomRight.xyz, level)
+    uint64_t* cell_code = nullptr;           // (1 << 3 level) | prefix
+    // internal node lookup by code
+    uint64_t* hkeys = nullptr;
+    int32_t* hvals = nullptr;
+    // radix sort
+    int32_t* hist = nullptr;                 // [digit][tile]
+    uint32_t* ghist = nullptr;               // [pass][digit]
+    int32_t* plan = nullptr;                 // [0..7] skip, [8..15] source buffer, [16] final buffer
+    int32_t* scan_sums = nullptr;
+    // counters (device) and their pinned host mirror
+    int32_t* counters = nullptr;
+    int32_t* h_counters = nullptr;
     unsigned long long* interactions = nullptr;
+    // host view of the last build
+    int n_in = 0, n_int = 0, n_cells = 0, final_buf = 0;
+    bool trivial = false;                    // < 2 bodies in the tree: all forces zero
+};
+
+// Tree counters (TreeBuffers::counters)
+enum : int {
+    TC_NIN = 0,       // bodies inside the root cube
+    TC_NINT = 1,      // internal nodes
+    TC_NLEAF = 2,     // leaf cells
+    TC_GAPS = 3,      // bodies whose path met a gap between float child bounds
+    TC_DEEPER = 4,    // depth-cap buckets whose bodies differ (the reference would split further)
+    TC_HASHFAIL = 5,  // failed internal-node lookups (must stay 0)
+    TC_COUNT = 8
 };
 
 // Phases timed by the per-handle profiler (NB_PHASE_* in the public header).

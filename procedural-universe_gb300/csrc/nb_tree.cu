@@ -1,8 +1,764 @@
-// placeholder, replaced by the octree build
+// nb_tree.cu -- Barnes-Hut octree build on the GPU: K2 keys, K3 radix sort,
+// K4 topology, K5 bottom-up mass and centre of mass.
+//
+// Replaces the serial pointer octree of BarnesHut::Update
+// (src/Sim/BarnesHut.cpp:44-56) and Octree::Split/Add/CalculateMass
+// (src/Sim/Octree.cpp:16-105) with the same tree, built in parallel:
+//
+//  * K2: a body's key is the octant path Octree::Add takes from the root,
+//    3 bits per level, octant = x + 2y + 4z (src/Sim/Octree.cpp:25-41).  The
+//    child bounds are replayed in float exactly as Split computes them
+//    (cur += size, BottomRight = cur + size, Size = BottomRight.x - TopLeft.x),
+//    with the half-open containment of BoundingCube::Contains
+//    (src/Sim/Octree.hpp:18-22).  A body outside the root cube gets key ~0:
+//    the reference drops it from the tree but counts it in the root.
+//  * K3: stable LSD radix sort of (key, body) pairs, 8 passes of 8 bits
+//    (reduce-then-scan; the scatter ranks digits with warp match_any).
+//    Passes whose digit is the same for every key are skipped on the device.
+//  * K4: the reference tree splits a node when a second body arrives and
+//    creates all 8 children, so its internal nodes are exactly the key
+//    prefixes shared by at least two bodies (and the root whenever it holds
+//    two bodies, dropped ones included).  With sorted keys, delta(s) = the
+//    number of leading octants bodies s and s+1 share; position s starts the
+//    internal nodes of levels delta(s-1)+1 .. min(delta(s), D-1) and one
+//    leaf.  Internal nodes are numbered by (first body, level) through a
+//    prefix sum; a node whose parent starts at an earlier body finds it in a
+//    hash table keyed by (1 << 3 level) | prefix.  Each internal node stores
+//    only its non-empty children, as consecutive cells in octant order
+//    (empty children hold no mass and contribute exactly zero force).
+//  * Depth cap D (max_depth, 21 = 63-bit keys): bodies sharing all D octants
+//    form one leaf (a bucket).  A bucket's mass and centre of mass sum its
+//    bodies in ascending body index (stable sort order).
+//  * K5: CalculateMass in the same arithmetic: TotalMass is a double sum of
+//    the children in octant order, CentreOfMass += child COM * float(child
+//    mass) in float, then scaled by 1.f / float(TotalMass).  Nodes are
+//    finished bottom-up: the last child to arrive finishes its parent.
+#include "nb_common.cuh"
 #include "nb_internal.hpp"
+#include "nb_scan.cuh"
+#include <algorithm>
+#include <cstring>
+
 namespace nb {
-cudaError_t tree_reserve(nb_sim*) { return cudaSuccess; }
-void tree_free(nb_sim*) {}
-cudaError_t tree_build(nb_sim*) { return cudaErrorNotSupported; }
-cudaError_t tree_forces(nb_sim*) { return cudaErrorNotSupported; }
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
+constexpr int kPasses = 8;
+constexpr int kEmitBlock = 256;
+
+enum : int { KIND_SINGLE = 1, KIND_BUCKET = 2, KIND_INTERNAL = 3 };
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
+
+// ---------------------------------------------------------------- K2 keys --
+__global__ void k_keys(const float4* __restrict__ pos, int n, int nk, float half, int D,
+                       uint64_t* __restrict__ keys, int32_t* __restrict__ vals, int32_t* __restrict__ depth,
+                       int32_t* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nk) return;
+    vals[i] = i;
+    bool inside = false, gap = false;
+    if (i < n) {
+        const float4 p = pos[i];
+        float lo0 = -half, lo1 = -half, lo2 = -half, hi0 = half, hi1 = half, hi2 = half;
+        inside = p.x >= lo0 && p.y >= lo1 && p.z >= lo2 && p.x < hi0 && p.y < hi1 && p.z < hi2;
+        uint64_t key = ~0ull;
+        int d = 0;
+        if (inside) {
+            key = 0;
+            float size = __fsub_rn(hi0, lo0);
+            for (int l = 0; l < D; ++l) {
+                const float s = __fdiv_rn(size, 2.0f);
+                const float m0 = __fadd_rn(lo0, s), m1 = __fadd_rn(lo1, s), m2 = __fadd_rn(lo2, s);
+                const float t0 = __fadd_rn(m0, s), t1 = __fadd_rn(m1, s), t2 = __fadd_rn(m2, s);
+                int oct = 0;
+                bool ok = true;
+                if (p.x >= m0 && p.x < t0) { oct |= 1; lo0 = m0; hi0 = t0; }
+                else if (p.x >= lo0 && p.x < m0) { hi0 = m0; }
+                else ok = false;
+                if (p.y >= m1 && p.y < t1) { oct |= 2; lo1 = m1; hi1 = t1; }
+                else if (p.y >= lo1 && p.y < m1) { hi1 = m1; }
+                else ok = false;
+                if (p.z >= m2 && p.z < t2) { oct |= 4; lo2 = m2; hi2 = t2; }
+                else if (p.z >= lo2 && p.z < m2) { hi2 = m2; }
+                else ok = false;
+                if (!ok) break;
+                size = __fsub_rn(hi0, lo0);
+                key = (key << 3) | (uint64_t)oct;
+                ++d;
+            }
+            if (d < D) {   // a gap between float child bounds: left-align the path
+                key <<= 3 * (D - d);
+                gap = true;
+            }
+        }
+        keys[i] = key;
+        depth[i] = d;
+    } else {
+        keys[i] = ~0ull;
+    }
+    const uint32_t in_b = __ballot_sync(0xffffffffu, inside);
+    const uint32_t gap_b = __ballot_sync(0xffffffffu, gap);
+    if ((threadIdx.x & 31) == 0) {
+        if (in_b) atomicAdd(&counters[TC_NIN], __popc(in_b));
+        if (gap_b) atomicAdd(&counters[TC_GAPS], __popc(gap_b));
+    }
+}
+
+// ------------------------------------------------------------ K3 radix sort --
+__global__ void __launch_bounds__(kSortThreads) k_sort_ghist(const uint64_t* __restrict__ keys,
+                                                             uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t h[kPasses][256];
+    for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile + threadIdx.x;
+    for (int it = 0; it < kSortItems; ++it) {
+        const uint64_t k = keys[base + it * kSortThreads];
+#pragma unroll
+        for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) {
+        const uint32_t v = (&h[0][0])[i];
+        if (v) atomicAdd(&ghist[i], v);
+    }
+}
+
+// plan[p] = 1 when every key has the same digit in pass p; plan[8+p] = buffer
+// the pass reads; plan[16] = buffer holding the result.
+__global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t* __restrict__ plan) {
+    __shared__ int triv[kPasses];
+    for (int p = 0; p < kPasses; ++p) {
+        const int t = __syncthreads_or(ghist[p * 256 + threadIdx.x] == (uint32_t)nk);
+        if (threadIdx.x == 0) triv[p] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int cur = 0;
+        for (int p = 0; p < kPasses; ++p) {
+            plan[p] = triv[p];
+            plan[8 + p] = cur;
+            if (!triv[p]) cur ^= 1;
+        }
+        plan[16] = cur;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_hist(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+                                                            int ntiles, const int32_t* __restrict__ plan, int pass,
+                                                            int32_t* __restrict__ hist) {
+    if (plan[pass]) return;
+    const uint64_t* keys = plan[8 + pass] ? k1 : k0;
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int shift = 8 * pass;
+    const int base = blockIdx.x * kSortTile + threadIdx.x;
+    for (int it = 0; it < kSortItems; ++it) atomicAdd(&h[(keys[base + it * kSortThreads] >> shift) & 255], 1u);
+    __syncthreads();
+    hist[threadIdx.x * ntiles + blockIdx.x] = (int32_t)h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+                                                               int32_t* __restrict__ v0, int32_t* __restrict__ v1,
+                                                               int ntiles, const int32_t* __restrict__ hist,
+                                                               const int32_t* __restrict__ plan, int pass) {
+    if (plan[pass]) return;
+    const int src = plan[8 + pass];
+    const uint64_t* ks = src ? k1 : k0;
+    uint64_t* kd = src ? k0 : k1;
+    const int32_t* vs = src ? v1 : v0;
+    int32_t* vd = src ? v0 : v1;
+    __shared__ uint32_t whist[kSortWarps][256];
+    __shared__ int32_t gbase[256];
+    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int shift = 8 * pass;
+    const int base = blockIdx.x * kSortTile + warp * (32 * kSortItems) + lane;
+    uint64_t k[kSortItems];
+    int32_t v[kSortItems];
+    uint32_t r[kSortItems];
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        k[it] = ks[base + it * 32];
+        v[it] = vs[base + it * 32];
+    }
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t b = whist[warp][d];
+        r[it] = b + __popc(peers & lt);
+        __syncwarp();
+        if (lane == 31 - __clz(peers)) whist[warp][d] = b + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = whist[w][d];
+            whist[w][d] = run;
+            run += c;
+        }
+        gbase[d] = hist[d * ntiles + blockIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
+        const int dst = gbase[d] + (int)whist[warp][d] + (int)r[it];
+        kd[dst] = k[it];
+        vd[dst] = v[it];
+    }
+}
+
+// --------------------------------------------------------- K4 topology ----
+__device__ __forceinline__ int lcp_levels(uint64_t a, uint64_t b, int D) {
+    const uint64_t x = a ^ b;
+    if (x == 0) return D;
+    return (__clzll((long long)x) - (64 - 3 * D)) / 3;
+}
+
+struct TopoView {
+    const uint64_t* keys;     // sorted
+    const int32_t* vals;      // body index per sorted position
+    const int32_t* depth;     // per body (input order)
+    int n_in, n_total, D;
+    __device__ int delta(int s) const {   // common levels of sorted bodies s and s+1; -1 past the end
+        if (s < 0 || s + 1 >= n_in) return -1;
+        int l = lcp_levels(keys[s], keys[s + 1], D);
+        l = min(l, depth[vals[s]]);
+        l = min(l, depth[vals[s + 1]]);
+        return l;
+    }
+    // Nodes starting at sorted position s: internal levels lo..hi and a leaf at
+    // level lf (lf = -1: s lies inside an earlier bucket).
+    __device__ void info(int s, int& lo, int& hi, int& nint, int& lf, int& cur) const {
+        const int prev = (s > 0) ? delta(s - 1) : -1;
+        cur = delta(s);
+        if (prev >= D) { lo = 0; hi = -1; nint = 0; lf = -1; return; }
+        lo = prev + 1;
+        hi = min(cur, D - 1);
+        if (s == 0 && n_total >= 2) hi = max(hi, 0);
+        nint = max(0, hi - lo + 1);
+        lf = nint > 0 ? hi + 1 : lo;
+    }
+};
+
+__device__ __forceinline__ uint64_t node_code(uint64_t key, int level, int D) {
+    return (1ull << (3 * level)) | (level ? (key >> (3 * (D - level))) : 0ull);
+}
+
+__device__ __forceinline__ uint32_t hash_slot(uint64_t code, uint32_t mask) {
+    uint64_t x = code * 0x9E3779B97F4A7C15ull;
+    x ^= x >> 29;
+    return (uint32_t)x & mask;
+}
+
+__device__ void hash_insert(uint64_t* hk, int32_t* hv, uint32_t mask, uint64_t code, int32_t val, int32_t* counters) {
+    uint32_t h = hash_slot(code, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long prev = atomicCAS((unsigned long long*)&hk[h], 0ull, (unsigned long long)code);
+        if (prev == 0ull || prev == code) {
+            hv[h] = val;
+            return;
+        }
+        h = (h + 1) & mask;
+    }
+    atomicAdd(&counters[TC_HASHFAIL], 1);
+}
+
+__device__ int32_t hash_find(const uint64_t* hk, const int32_t* hv, uint32_t mask, uint64_t code, int32_t* counters) {
+    uint32_t h = hash_slot(code, mask);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const uint64_t k = hk[h];
+        if (k == code) return hv[h];
+        if (k == 0ull) break;
+        h = (h + 1) & mask;
+    }
+    atomicAdd(&counters[TC_HASHFAIL], 1);
+    return 0;
+}
+
+// Bounds of the node with the given code, replaying Octree::Split in float.
+__device__ void node_bounds(uint64_t code, int level, float half, float3& lo, float3& hi, float& side) {
+    lo = make_float3(-half, -half, -half);
+    hi = make_float3(half, half, half);
+    float size = __fsub_rn(hi.x, lo.x);
+    for (int l = 1; l <= level; ++l) {
+        const int dg = (int)((code >> (3 * (level - l))) & 7ull);
+        const float s = __fdiv_rn(size, 2.0f);
+        const float mx = __fadd_rn(lo.x, s), my = __fadd_rn(lo.y, s), mz = __fadd_rn(lo.z, s);
+        if (dg & 1) { lo.x = mx; hi.x = __fadd_rn(mx, s); } else { hi.x = mx; }
+        if (dg & 2) { lo.y = my; hi.y = __fadd_rn(my, s); } else { hi.y = my; }
+        if (dg & 4) { lo.z = mz; hi.z = __fadd_rn(mz, s); } else { hi.z = mz; }
+        size = __fsub_rn(hi.x, lo.x);
+    }
+    side = size;
+}
+
+__global__ void k_gather(const float4* __restrict__ pos, const int32_t* __restrict__ vals, int n,
+                         float4* __restrict__ spos) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) {
+        const int v = vals[s];
+        spos[s] = (v >= 0 && v < n) ? pos[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+__global__ void k_positions(TopoView tv, const float4* __restrict__ spos, int32_t* __restrict__ pos_nint,
+                            int32_t* __restrict__ leaf_level, int32_t* __restrict__ leaf_count,
+                            int32_t* __restrict__ counters) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    bool leaf = false, deeper = false;
+    if (s < tv.n_total) {
+        tv.n_in = counters[TC_NIN];
+        int lo, hi, nint, lf, cur;
+        if (s < tv.n_in) {
+            tv.info(s, lo, hi, nint, lf, cur);
+        } else {
+            nint = 0; lf = -1; cur = -1;
+        }
+        int count = 0;
+        if (lf >= 0) {
+            count = 1;
+            if (lf == tv.D && cur == tv.D) {
+                int x = s;
+                const float4 p0 = spos[s];
+                while (x + 1 < tv.n_in && tv.delta(x) == tv.D) {
+                    ++x;
+                    ++count;
+                    const float4 q = spos[x];
+                    if (q.x != p0.x || q.y != p0.y || q.z != p0.z) deeper = true;
+                }
+            }
+            leaf = true;
+        }
+        pos_nint[s] = nint;
+        leaf_level[s] = lf;
+        leaf_count[s] = count;
+    }
+    const uint32_t lb = __ballot_sync(0xffffffffu, leaf);
+    const uint32_t db = __ballot_sync(0xffffffffu, deeper);
+    if ((threadIdx.x & 31) == 0) {
+        if (lb) atomicAdd(&counters[TC_NLEAF], __popc(lb));
+        if (db) atomicAdd(&counters[TC_DEEPER], __popc(db));
+    }
+}
+
+__global__ void k_emit(TopoView tv, const int32_t* __restrict__ int_base, int32_t* __restrict__ int_level,
+                       int32_t* __restrict__ int_first, uint64_t* __restrict__ int_code, uint64_t* __restrict__ hk,
+                       int32_t* __restrict__ hv, uint32_t hmask, int32_t* __restrict__ counters) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= tv.n_in) return;
+    int lo, hi, nint, lf, cur;
+    tv.info(s, lo, hi, nint, lf, cur);
+    const uint64_t key = tv.keys[s];
+    const int base = int_base[s];
+    for (int l = lo; l <= hi; ++l) {
+        const int k = base + (l - lo);
+        const uint64_t code = node_code(key, l, tv.D);
+        int_level[k] = l;
+        int_first[k] = s;
+        int_code[k] = code;
+        hash_insert(hk, hv, hmask, code, k, counters);
+    }
+}
+
+__global__ void k_link_internal(const int32_t* __restrict__ int_level, const int32_t* __restrict__ int_first,
+                                const uint64_t* __restrict__ int_code, TopoView tv, int n_int,
+                                const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv, uint32_t hmask,
+                                int32_t* __restrict__ int_parent, uint32_t* __restrict__ int_mask,
+                                int32_t* __restrict__ int_nint, int32_t* __restrict__ counters) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_int || k == 0) return;
+    const int l = int_level[k];
+    const int s = int_first[k];
+    const uint64_t code = int_code[k];
+    const int prev = (s > 0) ? tv.delta(s - 1) : -1;
+    const int parent = (l > prev + 1) ? k - 1 : hash_find(hk, hv, hmask, code >> 3, counters);
+    int_parent[k] = parent;
+    atomicOr(&int_mask[parent], 1u << (unsigned)(code & 7ull));
+    atomicAdd(&int_nint[parent], 1);
+}
+
+__global__ void k_link_leaves(TopoView tv, const int32_t* __restrict__ int_base, const int32_t* __restrict__ leaf_level,
+                              const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv, uint32_t hmask,
+                              int32_t* __restrict__ leaf_parent, uint32_t* __restrict__ int_mask,
+                              int32_t* __restrict__ counters) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= tv.n_in) return;
+    const int lf = leaf_level[s];
+    if (lf <= 0) return;
+    int lo, hi, nint, lf2, cur;
+    tv.info(s, lo, hi, nint, lf2, cur);
+    const uint64_t code = node_code(tv.keys[s], lf, tv.D);
+    const int parent = nint > 0 ? int_base[s] + (lf - 1 - lo) : hash_find(hk, hv, hmask, code >> 3, counters);
+    leaf_parent[s] = parent;
+    atomicOr(&int_mask[parent], 1u << (unsigned)(code & 7ull));
+}
+
+__global__ void k_popc(const uint32_t* __restrict__ mask, int n_int, int32_t* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n_int) out[k] = __popc(mask[k]);
+}
+
+__device__ __forceinline__ int child_cell(const int32_t* int_block, const uint32_t* int_mask, int parent, int oct) {
+    return 1 + int_block[parent] + __popc(int_mask[parent] & ((1u << oct) - 1u));
+}
+
+__global__ void k_place_internal(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
+                                 const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
+                                 const int32_t* __restrict__ int_block, int n_int, float half,
+                                 int32_t* __restrict__ int_cell, int4* __restrict__ cell_meta,
+                                 float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
+                                 uint64_t* __restrict__ cell_code) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_int) return;
+    const uint64_t code = int_code[k];
+    const int l = int_level[k];
+    const int cell = (k == 0) ? 0 : child_cell(int_block, int_mask, int_parent[k], (int)(code & 7ull));
+    int_cell[k] = cell;
+    float3 lo, hi;
+    float side;
+    node_bounds(code, l, half, lo, hi, side);
+    const uint32_t m = int_mask[k];
+    cell_meta[cell] = make_int4(1 + int_block[k], 0, __float_as_int(side), KIND_INTERNAL | (__popc(m) << 4));
+    cell_lo[cell] = make_float4(lo.x, lo.y, lo.z, side);
+    cell_hi[cell] = make_float4(hi.x, hi.y, hi.z, (float)l);
+    cell_code[cell] = code;
+}
+
+__global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_level,
+                               const int32_t* __restrict__ leaf_count, const int32_t* __restrict__ leaf_parent,
+                               const uint32_t* __restrict__ int_mask, const int32_t* __restrict__ int_block,
+                               const float4* __restrict__ spos, float half, float4* __restrict__ cell_com,
+                               double* __restrict__ cell_mass, int4* __restrict__ cell_meta,
+                               float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
+                               uint64_t* __restrict__ cell_code) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= tv.n_in) return;
+    const int lf = leaf_level[s];
+    if (lf < 0) return;
+    const uint64_t code = node_code(tv.keys[s], lf, tv.D);
+    const int cell = (lf == 0) ? 0 : child_cell(int_block, int_mask, leaf_parent[s], (int)(code & 7ull));
+    float3 lo, hi;
+    float side;
+    node_bounds(code, lf, half, lo, hi, side);
+    const int count = leaf_count[s];
+    float4 com;
+    double M;
+    if (count == 1) {
+        // leaf with one body: CentreOfMass = P->Position, TotalMass = P->Mass
+        com = spos[s];
+        M = (double)com.w;
+    } else {
+        // depth-cap bucket: bodies in ascending index order
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        M = 0.0;
+        for (int q = s; q < s + count; ++q) {
+            const float4 p = spos[q];
+            M += (double)p.w;
+            const float mf = p.w;
+            cx = __fadd_rn(cx, __fmul_rn(p.x, mf));
+            cy = __fadd_rn(cy, __fmul_rn(p.y, mf));
+            cz = __fadd_rn(cz, __fmul_rn(p.z, mf));
+        }
+        if (M > 0.0) {
+            const float inv = __fdiv_rn(1.0f, (float)M);
+            cx = __fmul_rn(cx, inv); cy = __fmul_rn(cy, inv); cz = __fmul_rn(cz, inv);
+        }
+        com = make_float4(cx, cy, cz, (float)M);
+    }
+    com.w = (float)M;
+    cell_com[cell] = com;
+    cell_mass[cell] = M;
+    cell_meta[cell] = make_int4(s, count, __float_as_int(side), count == 1 ? KIND_SINGLE : KIND_BUCKET);
+    cell_lo[cell] = make_float4(lo.x, lo.y, lo.z, side);
+    cell_hi[cell] = make_float4(hi.x, hi.y, hi.z, (float)lf);
+    cell_code[cell] = code;
+}
+
+// ------------------------------------------------------------- K5 mass ----
+__device__ void finish_node(int k, const int32_t* int_cell, const int32_t* int_block, const uint32_t* int_mask,
+                            float4* cell_com, double* cell_mass, int4* cell_meta, int dropped) {
+    const int c = int_cell[k];
+    const int F = 1 + int_block[k];
+    const int nch = __popc(int_mask[k]);
+    double M = 0.0;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    int count = 0;
+    for (int j = 0; j < nch; ++j) {
+        const double mc = __ldcg(&cell_mass[F + j]);
+        const float4 cc = __ldcg(&cell_com[F + j]);
+        const int4 mt = __ldcg(&cell_meta[F + j]);
+        M += mc;
+        const float mf = (float)mc;
+        cx = __fadd_rn(cx, __fmul_rn(cc.x, mf));
+        cy = __fadd_rn(cy, __fmul_rn(cc.y, mf));
+        cz = __fadd_rn(cz, __fmul_rn(cc.z, mf));
+        count += mt.y;
+    }
+    if (M > 0.0) {
+        const float inv = __fdiv_rn(1.0f, (float)M);
+        cx = __fmul_rn(cx, inv); cy = __fmul_rn(cy, inv); cz = __fmul_rn(cz, inv);
+    }
+    if (k == 0) count += dropped;
+    __stcg(&cell_com[c], make_float4(cx, cy, cz, (float)M));
+    __stcg(&cell_mass[c], M);
+    int4 mt = __ldcg(&cell_meta[c]);
+    mt.y = count;
+    __stcg(&cell_meta[c], mt);
+}
+
+__global__ void k_mass(int n_int, const int32_t* __restrict__ int_parent, const int32_t* __restrict__ int_nint,
+                       int32_t* __restrict__ int_pending, const int32_t* __restrict__ int_cell,
+                       const int32_t* __restrict__ int_block, const uint32_t* __restrict__ int_mask,
+                       float4* __restrict__ cell_com, double* __restrict__ cell_mass, int4* __restrict__ cell_meta,
+                       int dropped) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_int || int_nint[k] != 0) return;
+    for (int guard = 0; guard < 64; ++guard) {   // a path has at most 22 internal nodes
+        finish_node(k, int_cell, int_block, int_mask, cell_com, cell_mass, cell_meta, dropped);
+        if (k == 0) return;
+        __threadfence();
+        const int p = int_parent[k];
+        const int old = atomicAdd(&int_pending[p], 1);
+        if (old != int_nint[p] - 1) return;
+        __threadfence();
+        k = p;
+    }
+}
+
+// --------------------------------------------------------------- host ----
+static cudaError_t grow(void** p, size_t bytes) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    return cudaMalloc(p, bytes);
+}
+
+#define NB_TRY(x)                               \
+    do {                                        \
+        cudaError_t e_ = (x);                   \
+        if (e_ != cudaSuccess) return e_;       \
+    } while (0)
+
+static cudaError_t reserve_bodies(nb_sim* sim, size_t nk) {
+    TreeBuffers& t = sim->tree;
+    if (nk <= t.body_cap) return cudaSuccess;
+    const size_t cap = nk;
+    NB_TRY(grow((void**)&t.keys[0], cap * 8));
+    NB_TRY(grow((void**)&t.keys[1], cap * 8));
+    NB_TRY(grow((void**)&t.vals[0], cap * 4));
+    NB_TRY(grow((void**)&t.vals[1], cap * 4));
+    NB_TRY(grow((void**)&t.depth, cap * 4));
+    NB_TRY(grow((void**)&t.spos, cap * 16));
+    NB_TRY(grow((void**)&t.pos_nint, cap * 4));
+    NB_TRY(grow((void**)&t.leaf_level, cap * 4));
+    NB_TRY(grow((void**)&t.leaf_count, cap * 4));
+    NB_TRY(grow((void**)&t.leaf_parent, cap * 4));
+    const size_t ntiles = cap / kSortTile;
+    t.hist_cap = 256 * ntiles;
+    NB_TRY(grow((void**)&t.hist, t.hist_cap * 4));
+    if (!t.ghist) NB_TRY(cudaMalloc(&t.ghist, kPasses * 256 * 4));
+    if (!t.plan) NB_TRY(cudaMalloc(&t.plan, 32 * 4));
+    if (!t.counters) NB_TRY(cudaMalloc(&t.counters, TC_COUNT * 4));
+    if (!t.h_counters) NB_TRY(cudaMallocHost(&t.h_counters, TC_COUNT * 4));
+    if (!t.interactions) NB_TRY(cudaMalloc(&t.interactions, sizeof(unsigned long long)));
+    t.body_cap = cap;
+    return cudaSuccess;
+}
+
+static cudaError_t reserve_scan(nb_sim* sim, size_t n) {
+    TreeBuffers& t = sim->tree;
+    const size_t need = (size_t)scan_blocks((int)n) + 1;
+    if (need <= t.scan_cap) return cudaSuccess;
+    NB_TRY(grow((void**)&t.scan_sums, need * 4));
+    t.scan_cap = need;
+    return cudaSuccess;
+}
+
+static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
+    TreeBuffers& t = sim->tree;
+    if (n_int > t.int_cap) {
+        const size_t cap = n_int + n_int / 4 + 64;
+        NB_TRY(grow((void**)&t.int_level, cap * 4));
+        NB_TRY(grow((void**)&t.int_first, cap * 4));
+        NB_TRY(grow((void**)&t.int_parent, cap * 4));
+        NB_TRY(grow((void**)&t.int_mask, cap * 4));
+        NB_TRY(grow((void**)&t.int_nint, cap * 4));
+        NB_TRY(grow((void**)&t.int_pending, cap * 4));
+        NB_TRY(grow((void**)&t.int_block, cap * 4));
+        NB_TRY(grow((void**)&t.int_cell, cap * 4));
+        NB_TRY(grow((void**)&t.int_code, cap * 8));
+        t.int_cap = cap;
+        size_t h = 1024;
+        while (h < 2 * cap) h <<= 1;
+        NB_TRY(grow((void**)&t.hkeys, h * 8));
+        NB_TRY(grow((void**)&t.hvals, h * 4));
+        t.hash_cap = h;
+    }
+    if (n_cells > t.cell_cap) {
+        const size_t cap = n_cells + n_cells / 4 + 64;
+        NB_TRY(grow((void**)&t.cell_com, cap * 16));
+        NB_TRY(grow((void**)&t.cell_meta, cap * 16));
+        NB_TRY(grow((void**)&t.cell_mass, cap * 8));
+        NB_TRY(grow((void**)&t.cell_lo, cap * 16));
+        NB_TRY(grow((void**)&t.cell_hi, cap * 16));
+        NB_TRY(grow((void**)&t.cell_code, cap * 8));
+        t.cell_cap = cap;
+    }
+    return reserve_scan(sim, std::max(n_int, (size_t)1));
+}
+
+cudaError_t tree_reserve(nb_sim* sim) {
+    const size_t nk = pad_up(std::max<size_t>(sim->n, 1), kSortTile);
+    NB_TRY(reserve_bodies(sim, nk));
+    return reserve_scan(sim, std::max(nk, (size_t)256 * (nk / kSortTile)));
+}
+
+void tree_free(nb_sim* sim) {
+    TreeBuffers& t = sim->tree;
+    void* ptrs[] = {t.keys[0], t.keys[1], t.vals[0], t.vals[1], t.depth, t.spos, t.pos_nint, t.leaf_level,
+                    t.leaf_count, t.leaf_parent, t.int_level, t.int_first, t.int_parent, t.int_mask, t.int_nint,
+                    t.int_pending, t.int_block, t.int_cell, t.int_code, t.cell_com, t.cell_meta, t.cell_mass,
+                    t.cell_lo, t.cell_hi, t.cell_code, t.hkeys, t.hvals, t.hist, t.ghist, t.plan, t.scan_sums,
+                    t.counters, t.interactions};
+    for (void* p : ptrs) cudaFree(p);
+    if (t.h_counters) cudaFreeHost(t.h_counters);
+    t = TreeBuffers{};
+}
+
+static TopoView topo_view(nb_sim* sim) {
+    TreeBuffers& t = sim->tree;
+    TopoView tv;
+    tv.keys = t.keys[t.final_buf];
+    tv.vals = t.vals[t.final_buf];
+    tv.depth = t.depth;
+    tv.n_in = t.n_in;
+    tv.n_total = (int)sim->n;
+    tv.D = sim->prm.max_depth;
+    return tv;
+}
+
+// Keys of the current positions into t.keys[0] (input order), t.vals[0] = identity.
+static cudaError_t launch_keys(nb_sim* sim, size_t nk) {
+    TreeBuffers& t = sim->tree;
+    PhaseScope ps(sim, NB_PHASE_KEYS);
+    k_keys<<<(unsigned)((nk + 255) / 256), 256, 0, sim->stream>>>(sim->pos, (int)sim->n, (int)nk,
+                                                                 sim->prm.bounds_half, sim->prm.max_depth,
+                                                                 t.keys[0], t.vals[0], t.depth, t.counters);
+    return cudaGetLastError();
+}
+
+cudaError_t tree_build(nb_sim* sim) {
+    TreeBuffers& t = sim->tree;
+    const int n = (int)sim->n;
+    const size_t nk = pad_up(std::max<size_t>(sim->n, 1), kSortTile);
+    const int ntiles = (int)(nk / kSortTile);
+    NB_TRY(tree_reserve(sim));
+    cudaStream_t st = sim->stream;
+    NB_TRY(cudaMemsetAsync(t.counters, 0, TC_COUNT * 4, st));
+    NB_TRY(launch_keys(sim, nk));
+    {
+        PhaseScope ps(sim, NB_PHASE_SORT, 2 + kPasses * 5);
+        NB_TRY(cudaMemsetAsync(t.ghist, 0, kPasses * 256 * 4, st));
+        k_sort_ghist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.ghist);
+        k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan);
+        for (int p = 0; p < kPasses; ++p) {
+            k_sort_hist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], ntiles, t.plan, p, t.hist);
+            NB_TRY(exclusive_scan(t.hist, t.hist, 256 * ntiles, t.scan_sums, nullptr, st, t.plan + p));
+            k_sort_scatter<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles,
+                                                            t.hist, t.plan, p);
+        }
+        NB_TRY(cudaGetLastError());
+    }
+    // The sort result's buffer is decided on the device; read the plan with the counters below.
+    {
+        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 3);
+        // Gather needs the final buffer: run it for both candidates' source after reading the plan.
+        NB_TRY(cudaMemcpyAsync(t.h_counters + 7, t.plan + 16, 4, cudaMemcpyDeviceToHost, st));
+        NB_TRY(cudaStreamSynchronize(st));
+        t.final_buf = t.h_counters[7];
+        k_gather<<<(n + 255) / 256, 256, 0, st>>>(sim->pos, t.vals[t.final_buf], n, t.spos);
+        TopoView tv = topo_view(sim);
+        k_positions<<<(n + 255) / 256, 256, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters);
+        NB_TRY(exclusive_scan(t.pos_nint, t.pos_nint, n, t.scan_sums, t.counters + TC_NINT, st));
+        NB_TRY(cudaMemcpyAsync(t.h_counters, t.counters, TC_COUNT * 4 - 4, cudaMemcpyDeviceToHost, st));
+        NB_TRY(cudaStreamSynchronize(st));
+    }
+    t.n_in = t.h_counters[TC_NIN];
+    t.n_int = t.h_counters[TC_NINT];
+    t.n_cells = t.n_int + t.h_counters[TC_NLEAF];
+    t.trivial = (n < 2) || (t.n_in < 2 && t.n_int == 0) || t.n_in == 0;
+    if (t.trivial) return cudaSuccess;
+    NB_TRY(reserve_nodes(sim, (size_t)t.n_int, (size_t)t.n_cells));
+    TopoView tv = topo_view(sim);
+    const int ni = t.n_int;
+    const uint32_t hmask = (uint32_t)(t.hash_cap - 1);
+    {
+        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 6);
+        NB_TRY(cudaMemsetAsync(t.hkeys, 0, t.hash_cap * 8, st));
+        NB_TRY(cudaMemsetAsync(t.int_mask, 0, (size_t)ni * 4, st));
+        NB_TRY(cudaMemsetAsync(t.int_nint, 0, (size_t)ni * 4, st));
+        NB_TRY(cudaMemsetAsync(t.int_pending, 0, (size_t)ni * 4, st));
+        const int nbk = (t.n_in + kEmitBlock - 1) / kEmitBlock;
+        k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals,
+                                          hmask, t.counters);
+        k_link_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, ni, t.hkeys,
+                                                         t.hvals, hmask, t.int_parent, t.int_mask, t.int_nint,
+                                                         t.counters);
+        k_link_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask,
+                                                 t.leaf_parent, t.int_mask, t.counters);
+        k_popc<<<(ni + 255) / 256, 256, 0, st>>>(t.int_mask, ni, t.int_block);
+        NB_TRY(exclusive_scan(t.int_block, t.int_block, ni, t.scan_sums, nullptr, st));
+        k_place_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
+                                                          t.int_block, ni, sim->prm.bounds_half, t.int_cell,
+                                                          t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+        k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask,
+                                                  t.int_block, t.spos, sim->prm.bounds_half, t.cell_com,
+                                                  t.cell_mass, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+        NB_TRY(cudaGetLastError());
+    }
+    {
+        PhaseScope ps(sim, NB_PHASE_MASS);
+        k_mass<<<(ni + 255) / 256, 256, 0, st>>>(ni, t.int_parent, t.int_nint, t.int_pending, t.int_cell,
+                                                t.int_block, t.int_mask, t.cell_com, t.cell_mass, t.cell_meta,
+                                                n - t.n_in);
+        NB_TRY(cudaGetLastError());
+    }
+    sim->tree_valid = true;
+    return cudaSuccess;
+}
+
+cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal) {
+    if (cells) *cells = sim->tree.trivial ? 0 : sim->tree.n_cells;
+    if (internal) *internal = sim->tree.trivial ? 0 : sim->tree.n_int;
+    return cudaSuccess;
+}
+
+// Keys of the current positions in input order (for export).
+cudaError_t tree_keys_export(nb_sim* sim, uint64_t* d_keys, int32_t* d_depth) {
+    TreeBuffers& t = sim->tree;
+    const size_t nk = pad_up(std::max<size_t>(sim->n, 1), kSortTile);
+    NB_TRY(tree_reserve(sim));
+    NB_TRY(cudaMemsetAsync(t.counters, 0, TC_COUNT * 4, sim->stream));
+    NB_TRY(launch_keys(sim, nk));
+    NB_TRY(cudaMemcpyAsync(d_keys, t.keys[0], sim->n * 8, cudaMemcpyDeviceToDevice, sim->stream));
+    NB_TRY(cudaMemcpyAsync(d_depth, t.depth, sim->n * 4, cudaMemcpyDeviceToDevice, sim->stream));
+    sim->tree_valid = false;   // the sort buffers no longer match the tree
+    return cudaSuccess;
+}
+
+}  // namespace nb

@@ -121,6 +121,15 @@ def lib() -> ctypes.CDLL:
             "nb_diagnostics": ([vp, f32, vp], i32),
             "nb_stream": ([vp], vp),
             "nb_render_vertices": ([vp, vp, f32, vp, sz], i32),
+            "nb_tree_keys": ([vp, vp, vp], i32),
+            "nb_tree_size": ([vp, vp], i32),
+            "nb_tree_nodes": ([vp, vp, sz], i32),
+            "nb_tree_order": ([vp, vp], i32),
+            "nb_tree_stats": ([vp, vp], i32),
+            "nb_profile_enable": ([vp, i32], i32),
+            "nb_profile_read": ([vp, i32, vp, vp], i32),
+            "nb_launch_count": ([vp, vp], i32),
+            "nb_probe_fp32_peak": ([i32, vp], i32),
             "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
             "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
             "nb_seed_collision": ([ctypes.c_uint64, sz, f64, f64, f64, vp, vp], i32),
@@ -289,6 +298,31 @@ class NBodySim:
         return dict(kinetic=d.kinetic, potential=d.potential, total=d.total, momentum=np.array(d.momentum[:]),
                     angular_momentum=np.array(d.angular_momentum[:]), mass=d.mass,
                     centre_of_mass=np.array(d.centre_of_mass[:]))
+
+    # -- octree export (Barnes-Hut) --
+    def tree_keys(self):
+        k = np.zeros(self.n, np.uint64)
+        d = np.zeros(self.n, np.int32)
+        self._check(lib().nb_tree_keys(self._h, _ptr(k), _ptr(d)), "nb_tree_keys")
+        return k, d
+
+    def tree_nodes(self) -> np.ndarray:
+        m = ctypes.c_size_t(0)
+        self._check(lib().nb_tree_size(self._h, ctypes.byref(m)), "nb_tree_size")
+        out = np.zeros(m.value, TREE_NODE_DTYPE)
+        self._check(lib().nb_tree_nodes(self._h, _ptr(out), m.value), "nb_tree_nodes")
+        return out
+
+    def tree_order(self) -> np.ndarray:
+        o = np.zeros(self.n, np.int32)
+        self._check(lib().nb_tree_order(self._h, _ptr(o)), "nb_tree_order")
+        return o
+
+    def tree_stats(self) -> dict:
+        st = np.zeros(8, np.int64)
+        self._check(lib().nb_tree_stats(self._h, _ptr(st)), "nb_tree_stats")
+        return dict(inside=int(st[0]), internal=int(st[1]), nodes=int(st[2]), gaps=int(st[3]),
+                    deeper_buckets=int(st[4]), lookup_failures=int(st[5]), outside=int(st[6]))
 
     def render_vertices(self, colour: np.ndarray | None = None, scale: float = 1.0) -> np.ndarray:
         out = np.zeros(self.n, RENDER_DTYPE)
