@@ -52,8 +52,10 @@ TREE_NODE_DTYPE = np.dtype(
         ("lo", "<f4", (3,)),
         ("bucket_begin", "<i4"),
         ("bucket_end", "<i4"),
-    ]
+    ],
+    align=True,
 )
+assert TREE_NODE_DTYPE.itemsize == 72
 
 
 class nb_params(ctypes.Structure):

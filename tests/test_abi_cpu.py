@@ -45,6 +45,8 @@ def test_struct_layout_matches_c(tmp_path):
         " offsetof(nb_particle, forces), offsetof(nb_particle, mass), sizeof(nb_render_vertex));\n"
         'printf("%zu %zu %zu %zu\\n", sizeof(nb_params), offsetof(nb_params, stream), offsetof(nb_params, flags),'
         " sizeof(nb_diag));\n"
+        'printf("%zu %zu %zu\\n", sizeof(nb_tree_node), offsetof(nb_tree_node, mass),'
+        " offsetof(nb_tree_node, bucket_end));\n"
         "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-std=c99", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
@@ -56,6 +58,8 @@ def test_struct_layout_matches_c(tmp_path):
     assert vals[6] == nb.nb_params.stream.offset
     assert vals[7] == nb.nb_params.flags.offset
     assert vals[8] == ctypes.sizeof(nb.nb_diag)
+    d = nb.TREE_NODE_DTYPE
+    assert vals[9:12] == [d.itemsize, d.fields["mass"][1], d.fields["bucket_end"][1]]
 
 
 def test_default_params_translate_reference_constants():
