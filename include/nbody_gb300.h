@@ -216,6 +216,13 @@ int  nb_tree_stats(nb_sim* sim, int64_t* stats8);
 int  nb_profile_enable(nb_sim* sim, int on);      /* on != 0 clears the totals */
 /* Total milliseconds and launches of a phase since enabling (synchronises). */
 int  nb_profile_read(nb_sim* sim, int phase, double* total_ms, uint64_t* launches);
+/* Launch tuning of a handle's kernels (results are unchanged up to FP32
+ * summation order).  Keys: "direct_block" (64, 128, 256 threads),
+ * "direct_ipt" (1, 2, 4, 8 target bodies per thread), "direct_splits"
+ * (source ranges per target block, 0 = automatic), "traverse_bpl" (1 or 2
+ * bodies per lane).  Returns NB_EINVAL for an unknown key or value. */
+int  nb_tune(nb_sim* sim, const char* key, int value);
+int  nb_get_tune(nb_sim* sim, const char* key, int* value);
 /* Kernel launches issued by this handle since creation. */
 int  nb_launch_count(nb_sim* sim, uint64_t* launches);
 /* Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA) from

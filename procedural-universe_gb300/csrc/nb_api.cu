@@ -657,3 +657,42 @@ int nb_probe_fp32_peak(int device, double* tflops) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+int nb_tune(nb_sim* s, const char* key, int value) {
+    if (!s || !key) return NB_EINVAL;
+    const std::string k(key);
+    if (k == "direct_block") {
+        if (value != 64 && value != 128 && value != 256) return NB_EINVAL;
+        s->tune.block = value;
+    } else if (k == "direct_ipt") {
+        if (value != 1 && value != 2 && value != 4 && value != 8) return NB_EINVAL;
+        if (value == 8 && s->tune.block == 256) return NB_EINVAL;
+        s->tune.ipt = value;
+    } else if (k == "direct_splits") {
+        if (value < 0 || value > 4096) return NB_EINVAL;
+        s->tune.splits = value;
+    } else if (k == "traverse_bpl") {
+        if (value != 1 && value != 2) return NB_EINVAL;
+        s->trav_bpl = value;
+        return NB_OK;
+    } else {
+        return NB_EINVAL;
+    }
+    s->tune_set = true;
+    return NB_OK;
+}
+
+int nb_get_tune(nb_sim* s, const char* key, int* value) {
+    if (!s || !key || !value) return NB_EINVAL;
+    const std::string k(key);
+    if (k == "direct_block") *value = s->tune.block;
+    else if (k == "direct_ipt") *value = s->tune.ipt;
+    else if (k == "direct_splits") *value = s->tune.splits;
+    else if (k == "traverse_bpl") *value = s->trav_bpl;
+    else return NB_EINVAL;
+    return NB_OK;
+}
+
+}  // extern "C"

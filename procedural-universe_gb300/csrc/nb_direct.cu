@@ -275,6 +275,10 @@ static DirectTuning default_tuning(size_t n_pad) {
 
 cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     DirectTuning t = sim->tune;
+    if (!sim->tune_set) {
+        t = default_tuning(sim->n_pad);
+        t.splits = sim->tune.splits;
+    }
     if (t.block <= 0 || t.ipt <= 0) t = default_tuning(sim->n_pad);
     // A tuning whose target block does not divide the padded size falls back.
     if (sim->n_pad % (size_t)(t.block * t.ipt) != 0) t = default_tuning(sim->n_pad);

@@ -58,7 +58,9 @@ struct TreeBuffers {
     uint64_t* int_code = nullptr;            // (1 << 3 level) | prefix
     // per cell
     float4* cell_com = nullptr;              // (centre of mass, float(TotalMass))
-    int4* cell_meta = nullptr;               // (first child cell | first sorted body, count, side bits, kind | nchild << 4)
+    int4* cell_meta = nullptr;               // (first child cell | first sorted body, accept r^2, reject r^2,
+                                             //  kind | nchild << 4 | bucket count << 8)
+    int32_t* cell_count = nullptr;           // NumParticles
     double* cell_mass = nullptr;             // TotalMass
     float4* cell_lo = nullptr;               // (TopLeft.xyz, side)
     float4* cell_hi = nullptr;               // (BottomRight.xyz, level)
@@ -143,6 +145,8 @@ struct nb_sim {
     uint64_t inter_last = 0;
     bool forces_fresh = false;  // acc holds the forces of the current positions
     nb::Profiler prof{};
+    int trav_bpl = 2;          // bodies per lane of the traversal kernel (1 or 2)
+    bool tune_set = false;     // direct-sum tuning set through nb_tune (else sized by n)
     std::string err;
 };
 
@@ -170,6 +174,7 @@ void tree_free(nb_sim* sim);
 cudaError_t tree_build(nb_sim* sim);
 cudaError_t tree_forces(nb_sim* sim);
 cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal);
+float theta_float(double theta);   // smallest float >= theta
 
 // ---- profiling (nb_api.cu) ----
 // Records CUDA events around one phase on sim->stream when profiling is on

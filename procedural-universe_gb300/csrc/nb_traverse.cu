@@ -6,10 +6,11 @@
 //
 // A warp owns 32 consecutive bodies of the key-sorted order (spatially
 // close, so their walks mostly coincide).  The warp shares one node stack in
-// shared memory; an entry is (cell, lane mask): the lanes that decided to
-// open that cell.  Popping a cell, the warp visits its children; each lane in
-// the mask applies the reference's per-body rule to each child, so every
-// body makes exactly the decisions of the CPU recursion:
+// shared memory; an entry is (child range of a cell, lane mask): the lanes
+// that decided to open that cell.  Popping an entry, lanes 0..7 load the
+// cell's non-empty children (one coalesced load) into a per-warp shared
+// buffer, and each lane of the mask applies the reference's per-body rule to
+// every child, so each body makes exactly the decisions of the CPU recursion:
 //   * a one-body leaf (NumParticles == 1): pairwise force unless it is the
 //     body itself (p != P; with the float bounds nesting exactly, the
 //     reference's !Bounds.Contains(p) holds for every other body);
@@ -17,10 +18,10 @@
 //     monopole (COM, TotalMass) acts, else an internal node is opened
 //     (__ballot_sync collects the lanes that open it into the pushed entry)
 //     and a depth-cap bucket acts body by body.
-// The comparison is the reference's float ratio against the double Theta,
-// i.e. d / r < theta_f with theta_f the smallest float >= Theta.  It is
-// decided from d^2 against theta_f^2 r^2 when that is clear by a 1e-5 margin,
-// else by the exactly rounded sqrt and division, so decisions are exact.
+// The opening test compares the float r^2 (computed as the reference does)
+// with the cell's precomputed accept / reject thresholds; only when r^2 falls
+// between them (a 2e-5 relative band) is the exactly rounded ratio
+// float(side / sqrtf(r^2)) compared with theta_f, the smallest float >= Theta.
 // Forces are summed in FP32 per popped cell and folded into a Kahan total.
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
@@ -33,6 +34,7 @@ constexpr int kTravBlock = 128;
 constexpr int kTravWarps = kTravBlock / 32;
 constexpr int kStack = 176;   // >= 7 * 21 + 8 entries: the deepest possible walk
 constexpr float kTravTiny = 1e-30f;
+constexpr unsigned kRangeBits = 28;   // stack entry: first child cell (28 bits) | child count << 28
 
 enum : int { TK_SINGLE = 1, TK_BUCKET = 2, TK_INTERNAL = 3 };
 
@@ -52,125 +54,11 @@ __device__ __forceinline__ void pair_accel(float dx, float dy, float dz, float r
     az = fmaf(w, dz, az);
 }
 
-template <int LAW>
-__global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restrict__ spos,
-                                                         const int32_t* __restrict__ sorder, int n,
-                                                         const float4* __restrict__ cell_com,
-                                                         const int4* __restrict__ cell_meta, int n_cells,
-                                                         int max_pops, float theta_f,
-                                                         float th2, float S, float G, float4* __restrict__ acc,
-                                                         unsigned long long* __restrict__ inter,
-                                                         int* __restrict__ err) {
-    __shared__ int2 stk[kTravWarps][kStack];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int s = (blockIdx.x * kTravWarps + w) * 32 + lane;
-    const bool valid = s < n;
-    const float4 p = valid ? spos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    float tx = 0.f, ty = 0.f, tz = 0.f;
-    unsigned cnt = 0;
+}  // namespace nb
 
-    auto visit = [&](int c, bool mine) -> bool {
-        const float4 cm = __ldg(&cell_com[c]);
-        const int4 mt = __ldg(&cell_meta[c]);
-        const int kind = mt.w & 15;
-        bool open = false;
-        if (mine) {
-            if (kind == TK_SINGLE) {
-                if (mt.x != s) {
-                    const float dx = cm.x - p.x, dy = cm.y - p.y, dz = cm.z - p.z;
-                    pair_accel<LAW>(dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)), cm.w, S, tx, ty, tz);
-                    ++cnt;
-                }
-            } else {
-                const float dvx = __fsub_rn(p.x, cm.x), dvy = __fsub_rn(p.y, cm.y), dvz = __fsub_rn(p.z, cm.z);
-                const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dvx, dvx), __fmul_rn(dvy, dvy)), __fmul_rn(dvz, dvz));
-                const float side = __int_as_float(mt.z);
-                const float d2 = __fmul_rn(side, side);
-                const float t = __fmul_rn(th2, r2);
-                bool accept;
-                if (d2 < __fmul_rn(t, 0.99999f)) accept = true;
-                else if (d2 > __fmul_rn(t, 1.00001f)) accept = false;
-                else accept = __fdiv_rn(side, __fsqrt_rn(r2)) < theta_f;
-                if (accept) {
-                    if (cm.w != 0.f) {
-                        pair_accel<LAW>(-dvx, -dvy, -dvz, r2, cm.w, S, tx, ty, tz);
-                        ++cnt;
-                    }
-                } else if (kind == TK_INTERNAL) {
-                    open = true;
-                } else {
-                    const int qe = min(mt.x + mt.y, n);
-                    for (int q = max(mt.x, 0); q < qe; ++q) {
-                        if (q == s) continue;
-                        const float4 b = spos[q];
-                        const float dx = b.x - p.x, dy = b.y - p.y, dz = b.z - p.z;
-                        pair_accel<LAW>(dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)), b.w, S, tx, ty, tz);
-                        ++cnt;
-                    }
-                }
-            }
-        }
-        return open;
-    };
+#include "nb_traverse_kernel.cuh"
 
-    int top = 0;
-    bool overflow = false;
-    int pops = 0;
-    {
-        const unsigned om = __ballot_sync(0xffffffffu, visit(0, valid));
-        if (om) {
-            if (lane == 0) stk[w][0] = make_int2(0, (int)om);
-            top = 1;
-        }
-    }
-    __syncwarp();
-    while (top > 0) {
-        --top;
-        const int2 e = stk[w][top];
-        __syncwarp();
-        const bool mine = ((unsigned)e.y >> lane) & 1u;
-        const int4 pm = __ldg(&cell_meta[e.x]);
-        const int F = pm.x, nch = pm.w >> 4;
-        // A well-formed tree pops each internal cell at most once per warp and
-        // keeps child ranges inside the cell array; anything else is reported.
-        if (++pops > max_pops || F < 1 || nch > 8 || F + nch > n_cells) {
-            overflow = true;
-            break;
-        }
-        for (int j = 0; j < nch; ++j) {
-            const unsigned b = __ballot_sync(0xffffffffu, visit(F + j, mine));
-            if (b) {
-                if (top < kStack) {
-                    if (lane == 0) stk[w][top] = make_int2(F + j, (int)b);
-                    ++top;
-                } else {
-                    overflow = true;
-                }
-            }
-        }
-        __syncwarp();
-        kahan_add(sx, cx, tx);
-        kahan_add(sy, cy, ty);
-        kahan_add(sz, cz, tz);
-        tx = ty = tz = 0.f;
-        if (overflow) break;
-    }
-    kahan_add(sx, cx, tx);
-    kahan_add(sy, cy, ty);
-    kahan_add(sz, cz, tz);
-    if (overflow && lane == 0) record_error(err, DEV_STACK_OVERFLOW);
-    if (valid) acc[sorder[s]] = make_float4(G * (sx - cx), G * (sy - cy), G * (sz - cz), 0.f);
-    unsigned long long c = cnt;
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-    if (lane == 0 && c) atomicAdd(inter, c);
-}
-
-static float theta_float(double theta) {
-    float f = (float)theta;
-    if ((double)f < theta) f = std::nextafter(f, INFINITY);
-    return f;
-}
+namespace nb {
 
 cudaError_t tree_forces(nb_sim* sim) {
     TreeBuffers& t = sim->tree;
@@ -183,21 +71,21 @@ cudaError_t tree_forces(nb_sim* sim) {
     }
     const int n = (int)sim->n;
     const float tf = theta_float(sim->prm.theta);
-    const float th2 = tf * tf;
     const float S = (float)sim->prm.softening2;
     const float G = (float)sim->prm.G;
-    const int blocks = (n + kTravBlock - 1) / kTravBlock;
     PhaseScope ps(sim, NB_PHASE_TRAVERSE);
-    if (sim->prm.law == NB_LAW_PLUMMER)
-        k_traverse<NB_LAW_PLUMMER><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com,
-                                                                 t.cell_meta, t.n_cells, t.n_int + 1, tf, th2, S, G,
-                                                                 sim->acc,
-                                                                 t.interactions, sim->d_err);
-    else
-        k_traverse<NB_LAW_REFERENCE><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com,
-                                                                   t.cell_meta, t.n_cells, t.n_int + 1, tf, th2, S,
-                                                                   G, sim->acc,
-                                                                   t.interactions, sim->d_err);
+    const int bpl = sim->trav_bpl == 1 ? 1 : 2;
+    const int blocks = (n + kTravBlock * bpl - 1) / (kTravBlock * bpl);
+#define NB_TRAV(L, B)                                                                                          \
+    k_traverse<L, B><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com, t.cell_meta,   \
+                                                    t.cell_lo, t.n_cells, t.n_int + 1, tf, S, G, sim->acc,     \
+                                                    t.interactions, sim->d_err)
+    if (sim->prm.law == NB_LAW_PLUMMER) {
+        if (bpl == 1) NB_TRAV(NB_LAW_PLUMMER, 1); else NB_TRAV(NB_LAW_PLUMMER, 2);
+    } else {
+        if (bpl == 1) NB_TRAV(NB_LAW_REFERENCE, 1); else NB_TRAV(NB_LAW_REFERENCE, 2);
+    }
+#undef NB_TRAV
     return cudaGetLastError();
 }
 
@@ -287,8 +175,9 @@ int nb_tree_nodes(nb_sim* s, nb_tree_node* nodes, size_t capacity) {
     std::vector<int4> meta(C);
     std::vector<double> mass(C);
     std::vector<uint64_t> code(C);
-    std::vector<int32_t> order(s->n);
+    std::vector<int32_t> order(s->n), count(C);
     cudaError_t e = cudaMemcpy(com.data(), t.cell_com, C * 16, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(count.data(), t.cell_count, C * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(lo.data(), t.cell_lo, C * 16, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(hi.data(), t.cell_hi, C * 16, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(meta.data(), t.cell_meta, C * 16, cudaMemcpyDeviceToHost);
@@ -301,7 +190,7 @@ int nb_tree_nodes(nb_sim* s, nb_tree_node* nodes, size_t capacity) {
         const int level = (int)hi[c].w;
         const int kind = meta[c].w & 15;
         o.level = level;
-        o.count = meta[c].y;
+        o.count = count[c];
         o.first_child = kind == TK_INTERNAL ? meta[c].x : -1;
         o.body = kind == TK_SINGLE ? order[meta[c].x] : -1;
         o.prefix = level ? (code[c] & ((1ull << (3 * level)) - 1ull)) : 0ull;
@@ -310,7 +199,7 @@ int nb_tree_nodes(nb_sim* s, nb_tree_node* nodes, size_t capacity) {
         o.side = lo[c].w;
         o.lo[0] = lo[c].x; o.lo[1] = lo[c].y; o.lo[2] = lo[c].z;
         o.bucket_begin = kind == TK_BUCKET ? meta[c].x : -1;
-        o.bucket_end = kind == TK_BUCKET ? meta[c].x + meta[c].y : -1;
+        o.bucket_end = kind == TK_BUCKET ? meta[c].x + count[c] : -1;
     }
     return NB_OK;
 }

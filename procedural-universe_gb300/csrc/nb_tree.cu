@@ -37,6 +37,7 @@
 #include "nb_internal.hpp"
 #include "nb_scan.cuh"
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace nb {
@@ -414,13 +415,24 @@ __global__ void k_popc(const uint32_t* __restrict__ mask, int n_int, int32_t* __
     if (k < n_int) out[k] = __popc(mask[k]);
 }
 
+// Opening thresholds of a cell for the traversal: with r^2 computed exactly
+// as the reference does, r^2 > accept_r2 guarantees float(side / r) < theta_f
+// and r^2 < reject_r2 guarantees the opposite (1e-5 relative margins, far
+// above the float rounding of the ratio); between the two the traversal
+// evaluates the exactly rounded ratio.
+__device__ __forceinline__ void open_thresholds(float side, float theta_f, int& accept_bits, int& reject_bits) {
+    const double q = (double)side * (double)side / ((double)theta_f * (double)theta_f);
+    accept_bits = __float_as_int(__double2float_ru(q * (1.0 + 1e-5)));
+    reject_bits = __float_as_int(__double2float_rd(q * (1.0 - 1e-5)));
+}
+
 __device__ __forceinline__ int child_cell(const int32_t* int_block, const uint32_t* int_mask, int parent, int oct) {
     return 1 + int_block[parent] + __popc(int_mask[parent] & ((1u << oct) - 1u));
 }
 
 __global__ void k_place_internal(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
                                  const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
-                                 const int32_t* __restrict__ int_block, int n_int, float half,
+                                 const int32_t* __restrict__ int_block, int n_int, float half, float theta_f,
                                  int32_t* __restrict__ int_cell, int4* __restrict__ cell_meta,
                                  float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
                                  uint64_t* __restrict__ cell_code) {
@@ -434,7 +446,9 @@ __global__ void k_place_internal(const int32_t* __restrict__ int_level, const ui
     float side;
     node_bounds(code, l, half, lo, hi, side);
     const uint32_t m = int_mask[k];
-    cell_meta[cell] = make_int4(1 + int_block[k], 0, __float_as_int(side), KIND_INTERNAL | (__popc(m) << 4));
+    int ab, rb;
+    open_thresholds(side, theta_f, ab, rb);
+    cell_meta[cell] = make_int4(1 + int_block[k], ab, rb, KIND_INTERNAL | (__popc(m) << 4));
     cell_lo[cell] = make_float4(lo.x, lo.y, lo.z, side);
     cell_hi[cell] = make_float4(hi.x, hi.y, hi.z, (float)l);
     cell_code[cell] = code;
@@ -443,8 +457,9 @@ __global__ void k_place_internal(const int32_t* __restrict__ int_level, const ui
 __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_level,
                                const int32_t* __restrict__ leaf_count, const int32_t* __restrict__ leaf_parent,
                                const uint32_t* __restrict__ int_mask, const int32_t* __restrict__ int_block,
-                               const float4* __restrict__ spos, float half, float4* __restrict__ cell_com,
-                               double* __restrict__ cell_mass, int4* __restrict__ cell_meta,
+                               const float4* __restrict__ spos, float half, float theta_f,
+                               float4* __restrict__ cell_com, double* __restrict__ cell_mass,
+                               int32_t* __restrict__ cell_count, int4* __restrict__ cell_meta,
                                float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
                                uint64_t* __restrict__ cell_code) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -484,7 +499,10 @@ __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_lev
     com.w = (float)M;
     cell_com[cell] = com;
     cell_mass[cell] = M;
-    cell_meta[cell] = make_int4(s, count, __float_as_int(side), count == 1 ? KIND_SINGLE : KIND_BUCKET);
+    int ab, rb;
+    open_thresholds(side, theta_f, ab, rb);
+    cell_meta[cell] = make_int4(s, ab, rb, (count == 1 ? KIND_SINGLE : KIND_BUCKET) | (count << 8));
+    cell_count[cell] = count;
     cell_lo[cell] = make_float4(lo.x, lo.y, lo.z, side);
     cell_hi[cell] = make_float4(hi.x, hi.y, hi.z, (float)lf);
     cell_code[cell] = code;
@@ -492,7 +510,7 @@ __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_lev
 
 // ------------------------------------------------------------- K5 mass ----
 __device__ void finish_node(int k, const int32_t* int_cell, const int32_t* int_block, const uint32_t* int_mask,
-                            float4* cell_com, double* cell_mass, int4* cell_meta, int dropped) {
+                            float4* cell_com, double* cell_mass, int32_t* cell_count, int dropped) {
     const int c = int_cell[k];
     const int F = 1 + int_block[k];
     const int nch = __popc(int_mask[k]);
@@ -502,13 +520,13 @@ __device__ void finish_node(int k, const int32_t* int_cell, const int32_t* int_b
     for (int j = 0; j < nch; ++j) {
         const double mc = __ldcg(&cell_mass[F + j]);
         const float4 cc = __ldcg(&cell_com[F + j]);
-        const int4 mt = __ldcg(&cell_meta[F + j]);
+        const int cnt = __ldcg(&cell_count[F + j]);
         M += mc;
         const float mf = (float)mc;
         cx = __fadd_rn(cx, __fmul_rn(cc.x, mf));
         cy = __fadd_rn(cy, __fmul_rn(cc.y, mf));
         cz = __fadd_rn(cz, __fmul_rn(cc.z, mf));
-        count += mt.y;
+        count += cnt;
     }
     if (M > 0.0) {
         const float inv = __fdiv_rn(1.0f, (float)M);
@@ -517,20 +535,18 @@ __device__ void finish_node(int k, const int32_t* int_cell, const int32_t* int_b
     if (k == 0) count += dropped;
     __stcg(&cell_com[c], make_float4(cx, cy, cz, (float)M));
     __stcg(&cell_mass[c], M);
-    int4 mt = __ldcg(&cell_meta[c]);
-    mt.y = count;
-    __stcg(&cell_meta[c], mt);
+    __stcg(&cell_count[c], count);
 }
 
 __global__ void k_mass(int n_int, const int32_t* __restrict__ int_parent, const int32_t* __restrict__ int_nint,
                        int32_t* __restrict__ int_pending, const int32_t* __restrict__ int_cell,
                        const int32_t* __restrict__ int_block, const uint32_t* __restrict__ int_mask,
-                       float4* __restrict__ cell_com, double* __restrict__ cell_mass, int4* __restrict__ cell_meta,
-                       int dropped) {
+                       float4* __restrict__ cell_com, double* __restrict__ cell_mass,
+                       int32_t* __restrict__ cell_count, int dropped) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_int || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {   // a path has at most 22 internal nodes
-        finish_node(k, int_cell, int_block, int_mask, cell_com, cell_mass, cell_meta, dropped);
+        finish_node(k, int_cell, int_block, int_mask, cell_com, cell_mass, cell_count, dropped);
         if (k == 0) return;
         __threadfence();
         const int p = int_parent[k];
@@ -614,6 +630,7 @@ static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
         NB_TRY(grow((void**)&t.cell_com, cap * 16));
         NB_TRY(grow((void**)&t.cell_meta, cap * 16));
         NB_TRY(grow((void**)&t.cell_mass, cap * 8));
+        NB_TRY(grow((void**)&t.cell_count, cap * 4));
         NB_TRY(grow((void**)&t.cell_lo, cap * 16));
         NB_TRY(grow((void**)&t.cell_hi, cap * 16));
         NB_TRY(grow((void**)&t.cell_code, cap * 8));
@@ -633,11 +650,17 @@ void tree_free(nb_sim* sim) {
     void* ptrs[] = {t.keys[0], t.keys[1], t.vals[0], t.vals[1], t.depth, t.spos, t.pos_nint, t.leaf_level,
                     t.leaf_count, t.leaf_parent, t.int_level, t.int_first, t.int_parent, t.int_mask, t.int_nint,
                     t.int_pending, t.int_block, t.int_cell, t.int_code, t.cell_com, t.cell_meta, t.cell_mass,
-                    t.cell_lo, t.cell_hi, t.cell_code, t.hkeys, t.hvals, t.hist, t.ghist, t.plan, t.scan_sums,
+                    t.cell_lo, t.cell_hi, t.cell_code, t.cell_count, t.hkeys, t.hvals, t.hist, t.ghist, t.plan, t.scan_sums,
                     t.counters, t.interactions};
     for (void* p : ptrs) cudaFree(p);
     if (t.h_counters) cudaFreeHost(t.h_counters);
     t = TreeBuffers{};
+}
+
+float theta_float(double theta) {
+    float f = (float)theta;
+    if ((double)f < theta) f = std::nextafter(f, INFINITY);
+    return f;
 }
 
 static TopoView topo_view(nb_sim* sim) {
@@ -706,6 +729,7 @@ cudaError_t tree_build(nb_sim* sim) {
     NB_TRY(reserve_nodes(sim, (size_t)t.n_int, (size_t)t.n_cells));
     TopoView tv = topo_view(sim);
     const int ni = t.n_int;
+    const float tf = theta_float(sim->prm.theta);
     const uint32_t hmask = (uint32_t)(t.hash_cap - 1);
     {
         PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 6);
@@ -724,17 +748,18 @@ cudaError_t tree_build(nb_sim* sim) {
         k_popc<<<(ni + 255) / 256, 256, 0, st>>>(t.int_mask, ni, t.int_block);
         NB_TRY(exclusive_scan(t.int_block, t.int_block, ni, t.scan_sums, nullptr, st));
         k_place_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
-                                                          t.int_block, ni, sim->prm.bounds_half, t.int_cell,
+                                                          t.int_block, ni, sim->prm.bounds_half, tf, t.int_cell,
                                                           t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
         k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask,
-                                                  t.int_block, t.spos, sim->prm.bounds_half, t.cell_com,
-                                                  t.cell_mass, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+                                                  t.int_block, t.spos, sim->prm.bounds_half, tf, t.cell_com,
+                                                  t.cell_mass, t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi,
+                                                  t.cell_code);
         NB_TRY(cudaGetLastError());
     }
     {
         PhaseScope ps(sim, NB_PHASE_MASS);
         k_mass<<<(ni + 255) / 256, 256, 0, st>>>(ni, t.int_parent, t.int_nint, t.int_pending, t.int_cell,
-                                                t.int_block, t.int_mask, t.cell_com, t.cell_mass, t.cell_meta,
+                                                t.int_block, t.int_mask, t.cell_com, t.cell_mass, t.cell_count,
                                                 n - t.n_in);
         NB_TRY(cudaGetLastError());
     }

@@ -132,6 +132,8 @@ def lib() -> ctypes.CDLL:
             "nb_profile_read": ([vp, i32, vp, vp], i32),
             "nb_launch_count": ([vp, vp], i32),
             "nb_probe_fp32_peak": ([i32, vp], i32),
+            "nb_tune": ([vp, ctypes.c_char_p, i32], i32),
+            "nb_get_tune": ([vp, ctypes.c_char_p, vp], i32),
             "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
             "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
             "nb_seed_collision": ([ctypes.c_uint64, sz, f64, f64, f64, vp, vp], i32),
@@ -300,6 +302,14 @@ class NBodySim:
         return dict(kinetic=d.kinetic, potential=d.potential, total=d.total, momentum=np.array(d.momentum[:]),
                     angular_momentum=np.array(d.angular_momentum[:]), mass=d.mass,
                     centre_of_mass=np.array(d.centre_of_mass[:]))
+
+    def tune(self, key: str, value: int):
+        self._check(lib().nb_tune(self._h, key.encode(), int(value)), "nb_tune(%s=%d)" % (key, value))
+
+    def get_tune(self, key: str) -> int:
+        v = ctypes.c_int(0)
+        self._check(lib().nb_get_tune(self._h, key.encode(), ctypes.byref(v)), "nb_get_tune")
+        return v.value
 
     # -- octree export (Barnes-Hut) --
     def tree_keys(self):
