@@ -219,8 +219,8 @@ int  nb_profile_read(nb_sim* sim, int phase, double* total_ms, uint64_t* launche
 /* Launch tuning of a handle's kernels (results are unchanged up to FP32
  * summation order).  Keys: "direct_block" (64, 128, 256 threads),
  * "direct_ipt" (1, 2, 4, 8 target bodies per thread), "direct_splits"
- * (source ranges per target block, 0 = automatic), "traverse_bpl" (1 or 2
- * bodies per lane).  Returns NB_EINVAL for an unknown key or value. */
+ * (source ranges per target block, 0 = automatic).  Returns NB_EINVAL for
+ * an unknown key or value. */
 int  nb_tune(nb_sim* sim, const char* key, int value);
 int  nb_get_tune(nb_sim* sim, const char* key, int* value);
 /* Kernel launches issued by this handle since creation. */
@@ -228,6 +228,8 @@ int  nb_launch_count(nb_sim* sim, uint64_t* launches);
 /* Measured FP32 FMA throughput of the device (TFLOP/s, 2 flops per FMA) from
  * a dependent-chain FMA kernel filling every SM, timed with CUDA events. */
 int  nb_probe_fp32_peak(int device, double* tflops);
+/* The same with the packed FP32x2 FMA (FFMA2) of sm_100+, 4 flops per lane. */
+int  nb_probe_fp32x2_peak(int device, double* tflops);
 
 /* Headless render hand-off: fills n render vertices (LWParticle) with the
  * current positions and the given per-body colour (n x float4) and scale. */

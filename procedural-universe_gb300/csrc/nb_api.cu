@@ -673,10 +673,6 @@ int nb_tune(nb_sim* s, const char* key, int value) {
     } else if (k == "direct_splits") {
         if (value < 0 || value > 4096) return NB_EINVAL;
         s->tune.splits = value;
-    } else if (k == "traverse_bpl") {
-        if (value != 1 && value != 2) return NB_EINVAL;
-        s->trav_bpl = value;
-        return NB_OK;
     } else {
         return NB_EINVAL;
     }
@@ -690,9 +686,57 @@ int nb_get_tune(nb_sim* s, const char* key, int* value) {
     if (k == "direct_block") *value = s->tune.block;
     else if (k == "direct_ipt") *value = s->tune.ipt;
     else if (k == "direct_splits") *value = s->tune.splits;
-    else if (k == "traverse_bpl") *value = s->trav_bpl;
     else return NB_EINVAL;
     return NB_OK;
 }
 
 }  // extern "C"
+
+namespace nb {
+
+__global__ void k_fma2_probe(float* out, int iters, float a, float b) {
+    const float2 A = make_float2(a, a), B = make_float2(b, b);
+    float2 x0 = make_float2(threadIdx.x * 1e-3f, 1.f), x1 = make_float2(2.f, 3.f), x2 = make_float2(4.f, 5.f);
+    float2 x3 = make_float2(6.f, 7.f), x4 = make_float2(8.f, 9.f), x5 = make_float2(10.f, 11.f);
+    float2 x6 = make_float2(12.f, 13.f), x7 = make_float2(14.f, 15.f);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            x0 = __ffma2_rn(x0, A, B); x1 = __ffma2_rn(x1, A, B); x2 = __ffma2_rn(x2, A, B); x3 = __ffma2_rn(x3, A, B);
+            x4 = __ffma2_rn(x4, A, B); x5 = __ffma2_rn(x5, A, B); x6 = __ffma2_rn(x6, A, B); x7 = __ffma2_rn(x7, A, B);
+        }
+    }
+    const float r = ((x0.x + x1.x) + (x2.x + x3.x)) + ((x4.y + x5.y) + (x6.y + x7.y));
+    if (r == 1234.5678f) out[0] = r;
+}
+
+}  // namespace nb
+
+extern "C" int nb_probe_fp32x2_peak(int device, double* tflops) {
+    if (!tflops) return NB_EINVAL;
+    *tflops = 0.0;
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int threads = 512, blocks = sms * 4, iters = 4096;
+    nb::k_fma2_probe<<<blocks, threads>>>(d, 64, 1.0000001f, 1e-7f);
+    cudaEventRecord(a);
+    nb::k_fma2_probe<<<blocks, threads>>>(d, iters, 1.0000001f, 1e-7f);
+    cudaEventRecord(b);
+    cudaError_t e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    if (e != cudaSuccess || ms <= 0.f) { cudaGetLastError(); return NB_ECUDA; }
+    // 2 lanes x 2 flops per FFMA2
+    const double flops = 4.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return NB_OK;
+}

@@ -56,6 +56,36 @@ __device__ __forceinline__ void interact(const float4 pj, float xi, float yi, fl
     }
 }
 
+// The same interaction for two target bodies at once with the packed FP32x2
+// instructions of sm_100+ (FADD2 / FMUL2 / FFMA2): identical operations in
+// identical order, half the issue slots.  n* hold the negated target
+// coordinates, so dx = xj + (-xi) rounds exactly like xj - xi.
+template <int LAW>
+__device__ __forceinline__ void interact_x2(float2 jx, float2 jy, float2 jz, float2 jm, float2 nx, float2 ny,
+                                            float2 nz, float2 S2, float2& ax, float2& ay, float2& az) {
+    const float2 dx = __fadd2_rn(jx, nx);
+    const float2 dy = __fadd2_rn(jy, ny);
+    const float2 dz = __fadd2_rn(jz, nz);
+    float2 w;
+    if (LAW == NB_LAW_REFERENCE) {
+        float2 r2 = __fmul2_rn(dx, dx);
+        r2 = __ffma2_rn(dy, dy, r2);
+        r2 = __ffma2_rn(dz, dz, r2);
+        const float2 s = __fadd2_rn(r2, S2);
+        const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, make_float2(kTiny, kTiny));
+        w = __fmul2_rn(jm, make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y)));
+    } else {
+        float2 q = __ffma2_rn(dx, dx, S2);
+        q = __ffma2_rn(dy, dy, q);
+        q = __ffma2_rn(dz, dz, q);
+        const float2 inv = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+        w = __fmul2_rn(__fmul2_rn(jm, inv), __fmul2_rn(inv, inv));
+    }
+    ax = __ffma2_rn(w, dx, ax);
+    ay = __ffma2_rn(w, dy, ay);
+    az = __ffma2_rn(w, dz, az);
+}
+
 // K1: grid (target blocks, source ranges). Writes part[split][i] (sum) and
 // part[splits + split][i] (compensation).
 template <int LAW, int BLOCK, int IPT, bool COMP>
@@ -104,13 +134,39 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
 #pragma unroll 1
         for (int f = 0; f < kTileJ; f += kFold) {
             float tx[IPT], ty[IPT], tz[IPT];
+            if constexpr (IPT % 2 == 0) {
+                // Packed FP32x2: target bodies (2k, 2k+1) share every instruction.
+                constexpr int P = IPT / 2;
+                float2 ax[P], ay[P], az[P];
 #pragma unroll
-            for (int k = 0; k < IPT; ++k) tx[k] = ty[k] = tz[k] = 0.f;
+                for (int k = 0; k < P; ++k) ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
+                const float2 S2 = make_float2(S, S);
 #pragma unroll 4
-            for (int j = 0; j < kFold; ++j) {
-                const float4 pj = tj[f + j];
+                for (int j = 0; j < kFold; ++j) {
+                    const float4 pj = tj[f + j];
+                    const float2 jx = make_float2(pj.x, pj.x), jy = make_float2(pj.y, pj.y);
+                    const float2 jz = make_float2(pj.z, pj.z), jm = make_float2(pj.w, pj.w);
 #pragma unroll
-                for (int k = 0; k < IPT; ++k) interact<LAW>(pj, xi[k], yi[k], zi[k], S, tx[k], ty[k], tz[k]);
+                    for (int k = 0; k < P; ++k)
+                        interact_x2<LAW>(jx, jy, jz, jm, make_float2(-xi[2 * k], -xi[2 * k + 1]),
+                                         make_float2(-yi[2 * k], -yi[2 * k + 1]), make_float2(-zi[2 * k], -zi[2 * k + 1]),
+                                         S2, ax[k], ay[k], az[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < P; ++k) {
+                    tx[2 * k] = ax[k].x; tx[2 * k + 1] = ax[k].y;
+                    ty[2 * k] = ay[k].x; ty[2 * k + 1] = ay[k].y;
+                    tz[2 * k] = az[k].x; tz[2 * k + 1] = az[k].y;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) tx[k] = ty[k] = tz[k] = 0.f;
+#pragma unroll 4
+                for (int j = 0; j < kFold; ++j) {
+                    const float4 pj = tj[f + j];
+#pragma unroll
+                    for (int k = 0; k < IPT; ++k) interact<LAW>(pj, xi[k], yi[k], zi[k], S, tx[k], ty[k], tz[k]);
+                }
             }
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
@@ -251,7 +307,7 @@ int direct_splits(const nb_sim* sim, const DirectTuning& t, size_t n_pad) {
     const int iblocks = (int)(n_pad / (size_t)(t.block * t.ipt));
     int splits = t.splits;
     if (splits <= 0) {
-        const int target = std::max(1, sim->sm_count) * 24;   // many short units: dynamic balance
+        const int target = std::max(1, sim->sm_count) * 256;  // many short units: dynamic balance
         splits = (target + iblocks - 1) / iblocks;
         // keep the partials (2 float4 per body per split) within 512 MB
         const size_t cap = (512ull << 20) / (n_pad * 2 * sizeof(float4));
@@ -269,7 +325,7 @@ size_t direct_part_entries(const nb_sim* sim, const DirectTuning& t, size_t n_pa
 static DirectTuning default_tuning(size_t n_pad) {
     DirectTuning t;
     t.block = 128;
-    t.ipt = n_pad >= 65536 ? 4 : (n_pad >= 16384 ? 2 : 1);
+    t.ipt = n_pad >= 16384 ? 2 : 1;
     return t;
 }
 

@@ -145,7 +145,6 @@ struct nb_sim {
     uint64_t inter_last = 0;
     bool forces_fresh = false;  // acc holds the forces of the current positions
     nb::Profiler prof{};
-    int trav_bpl = 2;          // bodies per lane of the traversal kernel (1 or 2)
     bool tune_set = false;     // direct-sum tuning set through nb_tune (else sized by n)
     std::string err;
 };

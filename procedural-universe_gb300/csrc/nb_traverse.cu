@@ -74,17 +74,13 @@ cudaError_t tree_forces(nb_sim* sim) {
     const float S = (float)sim->prm.softening2;
     const float G = (float)sim->prm.G;
     PhaseScope ps(sim, NB_PHASE_TRAVERSE);
-    const int bpl = sim->trav_bpl == 1 ? 1 : 2;
-    const int blocks = (n + kTravBlock * bpl - 1) / (kTravBlock * bpl);
-#define NB_TRAV(L, B)                                                                                          \
-    k_traverse<L, B><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com, t.cell_meta,   \
-                                                    t.cell_lo, t.n_cells, t.n_int + 1, tf, S, G, sim->acc,     \
-                                                    t.interactions, sim->d_err)
-    if (sim->prm.law == NB_LAW_PLUMMER) {
-        if (bpl == 1) NB_TRAV(NB_LAW_PLUMMER, 1); else NB_TRAV(NB_LAW_PLUMMER, 2);
-    } else {
-        if (bpl == 1) NB_TRAV(NB_LAW_REFERENCE, 1); else NB_TRAV(NB_LAW_REFERENCE, 2);
-    }
+    const int blocks = (n + kTravBlock - 1) / kTravBlock;
+#define NB_TRAV(L)                                                                                          \
+    k_traverse<L><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com, t.cell_meta,   \
+                                                 t.cell_lo, t.n_cells, t.n_int + 1, tf, S, G, sim->acc,     \
+                                                 t.interactions, sim->d_err)
+    if (sim->prm.law == NB_LAW_PLUMMER) NB_TRAV(NB_LAW_PLUMMER);
+    else NB_TRAV(NB_LAW_REFERENCE);
 #undef NB_TRAV
     return cudaGetLastError();
 }

@@ -132,6 +132,7 @@ def lib() -> ctypes.CDLL:
             "nb_profile_read": ([vp, i32, vp, vp], i32),
             "nb_launch_count": ([vp, vp], i32),
             "nb_probe_fp32_peak": ([i32, vp], i32),
+            "nb_probe_fp32x2_peak": ([i32, vp], i32),
             "nb_tune": ([vp, ctypes.c_char_p, i32], i32),
             "nb_get_tune": ([vp, ctypes.c_char_p, vp], i32),
             "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
