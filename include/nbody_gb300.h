@@ -231,6 +231,33 @@ int  nb_probe_fp32_peak(int device, double* tflops);
 /* The same with the packed FP32x2 FMA (FFMA2) of sm_100+, 4 flops per lane. */
 int  nb_probe_fp32x2_peak(int device, double* tflops);
 
+/* ---- allocation-free direct sum -------------------------------------------- */
+/* No counterpart in the reference.  For callers that must not allocate device
+ * memory while they step: a render loop held to a fixed device-memory budget,
+ * a host whose buffers come from its own allocator, or a thread that must
+ * not stall (cudaFree synchronises the whole device).
+ *
+ * Accelerations of n bodies by direct summation (the handle path's kernels:
+ * Kahan-compensated FP32), enqueued on `stream` (cudaStream_t, NULL = the
+ * default stream) of the current device; nothing is allocated and nothing is
+ * read back.  pos_mass4: device buffer of n x (x, y, z, m); accel4: device
+ * buffer of n x (ax, ay, az, 0), G applied; both 16-byte aligned.  law:
+ * NB_LAW_*; softening2 = eps^2.
+ *
+ * Working memory: one fixed array of about 18 MB in every GPU's memory from
+ * the moment the library's kernels load there until the process exits.  It
+ * bounds n to NB_NOALLOC_MAX_BODIES; a larger n returns NB_EINVAL and
+ * enqueues nothing.  The first call on a device looks up the array's device
+ * address (once per device, with that device current); make that first call
+ * before any stream capture.  All calls on a device share the array, so calls
+ * whose work overlaps on the GPU (different streams, no ordering between
+ * them) race and give undefined results; calls on one stream are ordered.
+ * If a bounded device wait inside the kernels runs out, accel4 is filled
+ * with NaN. */
+#define NB_NOALLOC_MAX_BODIES 65536
+int  nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* accel4, double G, double softening2,
+                             int law, void* stream);
+
 /* Headless render hand-off: fills n render vertices (LWParticle) with the
  * current positions and the given per-body colour (n x float4) and scale. */
 int  nb_render_vertices(nb_sim* sim, const float* colour4, float scale, nb_render_vertex* out, size_t n);

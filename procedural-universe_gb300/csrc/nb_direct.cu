@@ -26,6 +26,7 @@
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
 #include <algorithm>
+#include <cmath>
 
 namespace nb {
 
@@ -396,3 +397,116 @@ cudaError_t kick_drift(nb_sim* sim, float dt) {
 }
 
 }  // namespace nb
+
+// ---------------------------------------------------------------------------
+// Allocation-free direct-sum accelerations.
+//
+// For callers that must not allocate device memory while they step: a render
+// loop that stays inside a fixed device-memory budget, a host that hands in
+// buffers owned by its own allocator, or a thread that must not block (every
+// cudaFree synchronises the whole device).  The caller passes device input
+// and output buffers; the working memory of the kernels is a file-scope
+// __device__ array of fixed size that every GPU loading this library holds
+// until the process exits.  It has no counterpart in the reference.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace nb {
+
+constexpr int kNoAllocMaxSplits = 8;
+// padded copy of the input + (sum, compensation) partials of up to 8 source ranges
+constexpr size_t kNoAllocScratch = (size_t)NB_NOALLOC_MAX_BODIES * (1 + 2 * kNoAllocMaxSplits);
+static __device__ __align__(256) float4 g_noalloc_scratch[kNoAllocScratch];   // 17.8 MB
+static __device__ int g_noalloc_err;
+
+// Copies n bodies into the scratch and zero-fills the padding (zero-mass
+// bodies at the origin contribute exactly nothing); clears the error word.
+__global__ void k_noalloc_stage(const float4* __restrict__ in, int n, int n_pad, float4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) g_noalloc_err = 0;
+    if (i < n_pad) out[i] = i < n ? in[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Folds the partials like k_direct_reduce_update; a force kernel whose bounded
+// wait ran out poisons the output with NaN, since nothing is read back.
+__global__ void k_noalloc_reduce(const float4* __restrict__ part, int splits, int n, int n_pad, float G,
+                                 float4* __restrict__ acc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+    for (int s = 0; s < splits; ++s) {
+        const float4 p = part[(size_t)s * n_pad + i];
+        const float4 c = part[(size_t)(splits + s) * n_pad + i];
+        kahan_add(ax, kx, p.x);
+        kahan_add(ay, ky, p.y);
+        kahan_add(az, kz, p.z);
+        qx += c.x; qy += c.y; qz += c.z;
+    }
+    float4 a = make_float4(G * (ax - (kx + qx)), G * (ay - (ky + qy)), G * (az - (kz + qz)), 0.f);
+    if (g_noalloc_err != 0) a = make_float4(NAN, NAN, NAN, NAN);
+    acc[i] = a;
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+float4* g_noalloc_ptr[256] = {};   // device address of the scratch, per device ordinal
+int* g_noalloc_err_ptr[256] = {};
+}  // namespace
+
+}  // namespace nb
+
+extern "C" int nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* accel4, double G, double softening2,
+                                       int law, void* stream) {
+    using namespace nb;
+    if (!pos_mass4 || !accel4 || n == 0) return NB_EINVAL;
+    if (n > (size_t)NB_NOALLOC_MAX_BODIES) return NB_EINVAL;
+    if (law != NB_LAW_REFERENCE && law != NB_LAW_PLUMMER) return NB_EINVAL;
+    if (!std::isfinite(G) || !std::isfinite(softening2) || softening2 < 0 ||
+        (law == NB_LAW_PLUMMER && softening2 <= 0))
+        return NB_EINVAL;
+    if ((reinterpret_cast<uintptr_t>(pos_mass4) | reinterpret_cast<uintptr_t>(accel4)) & 15u) return NB_EINVAL;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { cudaGetLastError(); return NB_ECUDA; }
+    float4* scratch = nullptr;
+    int* err = nullptr;
+    {
+        // Set-up on the first call on each device, with that device current.
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            void* q = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess ||
+                cudaGetSymbolAddress(&q, g_noalloc_err) != cudaSuccess || !p || !q) {
+                cudaGetLastError();
+                return NB_ECUDA;
+            }
+            g_noalloc_ptr[dev] = static_cast<float4*>(p);
+            g_noalloc_err_ptr[dev] = static_cast<int*>(q);
+        }
+        scratch = g_noalloc_ptr[dev];
+        err = g_noalloc_err_ptr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t n_pad = pad_up(n, kPad);
+    const int ntiles = (int)(n_pad / kTileJ);
+    int splits = std::min(kNoAllocMaxSplits, ntiles);
+    const int tps = (ntiles + splits - 1) / splits;
+    splits = (ntiles + tps - 1) / tps;
+    float4* pos = scratch;
+    float4* part = scratch + n_pad;
+    k_noalloc_stage<<<(unsigned)((n_pad + 255) / 256), 256, 0, st>>>(reinterpret_cast<const float4*>(pos_mass4),
+                                                                    (int)n, (int)n_pad, pos);
+    const int block = 128, ipt = n_pad >= 16384 ? 2 : 1;
+    dim3 grid((unsigned)(n_pad / (size_t)(block * ipt)), (unsigned)splits);
+    const float S = (float)softening2;
+    bool ok = law == NB_LAW_PLUMMER
+                  ? launch_force_law<NB_LAW_PLUMMER, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles, splits,
+                                                          S, part, err)
+                  : launch_force_law<NB_LAW_REFERENCE, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles,
+                                                            splits, S, part, err);
+    if (!ok) return NB_EINVAL;
+    k_noalloc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)n, (int)n_pad, (float)G,
+                                                                 reinterpret_cast<float4*>(accel4));
+    if (cudaGetLastError() != cudaSuccess) return NB_ECUDA;
+    return NB_OK;
+}

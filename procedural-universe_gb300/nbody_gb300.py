@@ -134,6 +134,7 @@ def lib() -> ctypes.CDLL:
             "nb_probe_fp32_peak": ([i32, vp], i32),
             "nb_probe_fp32x2_peak": ([i32, vp], i32),
             "nb_tune": ([vp, ctypes.c_char_p, i32], i32),
+            "nb_direct_accel_noalloc": ([vp, sz, vp, f64, f64, i32, vp], i32),
             "nb_get_tune": ([vp, ctypes.c_char_p, vp], i32),
             "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
             "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
