@@ -231,6 +231,43 @@ int  nb_probe_fp32_peak(int device, double* tflops);
 /* The same with the packed FP32x2 FMA (FFMA2) of sm_100+, 4 flops per lane. */
 int  nb_probe_fp32x2_peak(int device, double* tflops);
 
+/* ---- batched form: many independent galaxies, one launch per phase ------- */
+/* Galaxies with n >= bh_threshold use a group-wise Barnes-Hut (tight cube per
+ * galaxy, opening test side / distance(group box, COM) < bh_theta, monopole +
+ * quadrupole cells, leaf buckets of leaf_size bodies); the others use the
+ * direct sum.  Every phase is one launch over all galaxies, and a step is
+ * replayed from a captured CUDA graph.  Parity is the force error against the
+ * FP64 direct sum (<= 1e-3), not the reference's per-body opening rule. */
+typedef struct nb_batch nb_batch;
+typedef struct nb_tuning {
+    int direct_block;     /* threads per block of the direct-sum kernel (64, 128, 256) */
+    int direct_ipt;       /* target bodies per thread (1, 2; block * ipt <= 256)       */
+    int direct_jtile;     /* source bodies per work unit (multiple of 128)             */
+    int leaf_size;        /* bodies per Barnes-Hut leaf bucket (1..64)                  */
+    int traverse_block;   /* threads per block of the traversal kernel (128)           */
+} nb_tuning;
+/* base: law, G, softening2, pos_scale, device, stream of the batch. */
+int  nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta, nb_batch** out);
+int  nb_batch_destroy(nb_batch* b);
+const char* nb_batch_last_error(const nb_batch* b);
+/* Adds one galaxy (host buffers n x float4 each); galaxy receives its index. */
+int  nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t n, int32_t* galaxy);
+/* Uploads every galaxy, lays out the tables and sizes the tree buffers. */
+int  nb_batch_commit(nb_batch* b);
+int  nb_batch_set_tuning(nb_batch* b, const nb_tuning* t);
+int  nb_batch_get_tuning(nb_batch* b, nb_tuning* t);
+/* Project autotuner: times candidate leaf sizes, then candidate direct-sum
+ * tilings, for trial_steps graph replays each (state restored after each
+ * trial) and keeps the fastest. */
+int  nb_batch_autotune(nb_batch* b, float dt, int trial_steps);
+/* nsteps kick-drift steps of every galaxy, replayed from a captured CUDA graph. */
+int  nb_batch_step(nb_batch* b, float dt, int nsteps);
+int  nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4);
+/* Forces (n x 3 doubles) of one galaxy at the current state. */
+int  nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3);
+int  nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last);
+void* nb_batch_stream(nb_batch* b);
+
 /* ---- allocation-free direct sum -------------------------------------------- */
 /* No counterpart in the reference.  For callers that must not allocate device
  * memory while they step: a render loop held to a fixed device-memory budget,

@@ -1,0 +1,610 @@
+// nb_batch.cu -- batched form: many independent galaxies stepped together,
+// one launch per phase, the whole step replayed from a captured CUDA graph,
+// launch parameters chosen by the project's autotuner.  Kernels: see
+// nb_batch_kernels.cuh.
+#include "nb_common.cuh"
+#include "nb_internal.hpp"
+#include "nb_law.cuh"
+#include "nb_batch_kernels.cuh"
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace nb;
+
+struct nb_batch {
+    nb_params base{};
+    size_t bh_threshold = 8192;
+    double bh_theta = 0.6;
+    nb_sim* core = nullptr;   // device state of all bodies, stream, error word, tree buffers
+    std::string err;
+    // galaxies as added
+    struct Gal {
+        size_t n = 0;
+        bool bh = false;
+        size_t off = 0;   // first body in the concatenated arrays
+        int idx = -1;     // slot (Barnes-Hut) or direct-galaxy index
+        size_t n_pad = 0;
+    };
+    std::vector<Gal> gal;
+    std::vector<std::vector<float>> h_pos, h_vel;
+    bool committed = false;
+    size_t n_bh = 0, dir_begin = 0, n_total = 0, n_real = 0;
+    int nslot = 0, ndgal = 0;
+    // Barnes-Hut tables
+    int32_t* body_slot = nullptr;
+    int4* gal_range = nullptr;
+    float4* gal_box = nullptr;
+    int32_t* gal_root = nullptr;
+    int32_t* slot_start = nullptr;
+    int4* warps = nullptr;
+    int nwarps = 0;
+    float4* cell_q1 = nullptr;
+    float4* cell_q2 = nullptr;
+    int32_t* cell_first = nullptr;
+    size_t qcap = 0;
+    // direct-sum tables
+    int32_t* body_dgal = nullptr;
+    int4* dgal = nullptr;
+    int4* units = nullptr;
+    int32_t* unit_comp = nullptr;
+    int nunits = 0;
+    float4* part = nullptr;
+    size_t part_cap = 0;
+    int* next_unit = nullptr;
+    uint64_t direct_pairs = 0;
+    // tuning and graph
+    nb_tuning tune{128, 1, 1024, 16, 128};
+    cudaGraphExec_t exec = nullptr;
+    float graph_dt = NAN;
+    bool graph_dirty = true;
+    uint64_t graph_kernels = 0;
+};
+
+namespace {
+
+int bfail(nb_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define NB_BCUDA(b, call)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return bfail((b), NB_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& src) {
+    if (*dst) cudaFree(*dst);
+    *dst = nullptr;
+    if (src.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc(dst, src.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+bool tuning_valid(const nb_tuning& t) {
+    const bool blk = t.direct_block == 64 || t.direct_block == 128 || t.direct_block == 256;
+    const bool ipt = t.direct_ipt == 1 || t.direct_ipt == 2;
+    return blk && ipt && t.direct_block * t.direct_ipt <= 256 && t.direct_jtile >= 128 && t.direct_jtile % 128 == 0 && t.leaf_size >= 1 &&
+           t.leaf_size <= 64 && t.traverse_block == 128;
+}
+
+// Work units of the direct-sum galaxies for the current tuning.
+int plan_units(nb_batch* b) {
+    std::vector<int4> units, dg(b->ndgal);
+    std::vector<int32_t> ucomp;
+    const int tb = b->tune.direct_block * b->tune.direct_ipt;
+    const int utiles = b->tune.direct_jtile / kDirTile;
+    size_t part_base = 0;
+    for (const auto& g : b->gal) {
+        if (g.bh) continue;
+        const int ntiles = (int)(g.n_pad / kDirTile);
+        const int splits = (ntiles + utiles - 1) / utiles;
+        dg[g.idx] = make_int4((int)g.off, (int)g.n_pad, splits, (int)part_base);
+        const int comp = splits * (int)g.n_pad;
+        for (int blk = 0; blk < (int)(g.n_pad / tb); ++blk)
+            for (int s = 0; s < splits; ++s) {
+                const int t0 = s * utiles;
+                const int nt = std::min(utiles, ntiles - t0);
+                units.push_back(make_int4((int)g.off + blk * tb, (int)(g.off / kDirTile) + t0, nt,
+                                          (int)part_base + s * (int)g.n_pad + blk * tb));
+                ucomp.push_back(comp);
+            }
+        part_base += 2 * (size_t)splits * g.n_pad;
+    }
+    if (part_base > (size_t)INT32_MAX) return bfail(b, NB_ENOMEM, "direct-sum partials exceed 2^31 entries");
+    NB_BCUDA(b, upload(&b->units, units));
+    NB_BCUDA(b, upload(&b->unit_comp, ucomp));
+    NB_BCUDA(b, upload(&b->dgal, dg));
+    b->nunits = (int)units.size();
+    if (part_base > b->part_cap) {
+        cudaFree(b->part);
+        b->part = nullptr;
+        b->part_cap = 0;
+        NB_BCUDA(b, cudaMalloc(&b->part, std::max<size_t>(part_base, 1) * sizeof(float4)));
+        b->part_cap = part_base;
+    }
+    b->graph_dirty = true;
+    return NB_OK;
+}
+
+template <int LAW>
+bool launch_direct_t(nb_batch* b, int grid, cudaStream_t st, float S) {
+    const int blk = b->tune.direct_block, ipt = b->tune.direct_ipt;
+#define NB_BD(B, I)                                                                                           \
+    if (blk == B && ipt == I) {                                                                               \
+        k_batch_direct<LAW, B, I><<<grid, B, 0, st>>>(b->core->pos, b->units, b->unit_comp, b->nunits,         \
+                                                      b->next_unit, S, b->part);                              \
+        return true;                                                                                          \
+    }
+    NB_BD(64, 1) NB_BD(64, 2) NB_BD(128, 1) NB_BD(128, 2) NB_BD(256, 1)
+#undef NB_BD
+    return false;
+}
+
+// One step (update) or one force evaluation (no update) of every galaxy,
+// enqueued on the core stream without host synchronisation.
+int enqueue_step(nb_batch* b, float dt, bool update) {
+    nb_sim* c = b->core;
+    cudaStream_t st = c->stream;
+    const float S = (float)b->base.softening2;
+    const float G = (float)b->base.G;
+    TreeBuffers& t = c->tree;
+    NB_BCUDA(b, cudaMemsetAsync(t.interactions, 0, sizeof(unsigned long long), st));
+    if (b->n_bh > 0) {
+        const int n = (int)b->n_bh;
+        const size_t nk = pad_up((size_t)n, (size_t)tree_sort_tile());
+        {
+            PhaseScope ps(c, NB_PHASE_KEYS, 2);
+            k_gal_box<<<b->nslot, 256, 0, st>>>(c->pos, b->gal_range, b->nslot, b->gal_box);
+            k_batch_keys<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(c->pos, b->body_slot, n, (int)nk, b->gal_box,
+                                                                      t.keys[0], t.vals[0], t.depth);
+        }
+        NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth));
+        {
+            PhaseScope ps(c, NB_PHASE_MASS, 3);
+            NB_BCUDA(b, cudaMemsetAsync(t.int_pending, 0, t.int_cap * 4, st));
+            k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
+                (int)t.int_cap, t.counters + TC_NINT, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
+                t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_first,
+                t.cell_meta);
+            k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
+                                                                 t.int_cell, t.counters + TC_NINT, b->gal_root,
+                                                                 c->d_err);
+        }
+        {
+            PhaseScope ps(c, NB_PHASE_TRAVERSE);
+            const float th = (float)b->bh_theta;
+            const int blocks = (b->nwarps + kGWarps - 1) / kGWarps;
+#define NB_GT(L)                                                                                                  \
+    k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(b->warps, b->nwarps, t.spos, t.vals[0], t.cell_com,      \
+                                                        t.cell_meta, b->cell_q1, b->cell_q2, b->cell_first,      \
+                                                        t.cell_count, t.cell_hi, b->gal_box, b->gal_root,        \
+                                                        (int)t.cell_cap, (int)t.int_cap, b->tune.leaf_size,      \
+                                                        th * th, S, G, c->acc, t.interactions, c->d_err)
+            if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
+            else NB_GT(NB_LAW_REFERENCE);
+#undef NB_GT
+        }
+        NB_BCUDA(b, cudaGetLastError());
+    }
+    if (b->ndgal > 0) {
+        PhaseScope ps(c, NB_PHASE_DIRECT_FORCE, 2);
+        NB_BCUDA(b, cudaMemsetAsync(b->next_unit, 0, sizeof(int), st));
+        int occ = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_direct<NB_LAW_REFERENCE, 128, 1>,
+                                                      b->tune.direct_block, 0);
+        const int grid = std::max(1, std::min(b->nunits, c->sm_count * std::max(1, occ)));
+        const bool ok = b->base.law == NB_LAW_PLUMMER ? launch_direct_t<NB_LAW_PLUMMER>(b, grid, st, S)
+                                                      : launch_direct_t<NB_LAW_REFERENCE>(b, grid, st, S);
+        if (!ok) return bfail(b, NB_EINVAL, "unsupported direct tuning");
+        const int cnt = (int)(b->n_total - b->dir_begin);
+        k_batch_direct_reduce<<<(cnt + 255) / 256, 256, 0, st>>>(b->body_dgal, b->dgal, (int)b->dir_begin, cnt, G,
+                                                                b->part, c->acc);
+        NB_BCUDA(b, cudaGetLastError());
+    }
+    if (update) {
+        NB_BCUDA(b, kick_drift(c, dt));
+    }
+    return NB_OK;
+}
+
+int read_tree_counts(nb_batch* b, int32_t* h) {
+    NB_BCUDA(b, cudaMemcpyAsync(h, b->core->tree.counters, TC_COUNT * 4, cudaMemcpyDeviceToHost, b->core->stream));
+    NB_BCUDA(b, cudaStreamSynchronize(b->core->stream));
+    return NB_OK;
+}
+
+int reserve_tree(nb_batch* b, size_t n_int, size_t n_cells) {
+    if (b->n_bh == 0) return NB_OK;
+    NB_BCUDA(b, tree_reserve_graph(b->core, (int)b->n_bh, n_int, n_cells));
+    const size_t cap = b->core->tree.cell_cap;
+    if (cap > b->qcap) {
+        cudaFree(b->cell_q1); cudaFree(b->cell_q2); cudaFree(b->cell_first);
+        b->cell_q1 = b->cell_q2 = nullptr;
+        b->cell_first = nullptr;
+        NB_BCUDA(b, cudaMalloc(&b->cell_q1, cap * sizeof(float4)));
+        NB_BCUDA(b, cudaMalloc(&b->cell_q2, cap * sizeof(float4)));
+        NB_BCUDA(b, cudaMalloc(&b->cell_first, cap * sizeof(int32_t)));
+        b->qcap = cap;
+    }
+    b->graph_dirty = true;
+    return NB_OK;
+}
+
+// Sizes the tree capacity from measured counts (a synchronising force pass).
+int size_tree(nb_batch* b) {
+    if (b->n_bh == 0) return NB_OK;
+    size_t gi = 2 * b->n_bh + 64, gc = 3 * b->n_bh + 64;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        int rc = reserve_tree(b, gi, gc);
+        if (rc) return rc;
+        rc = enqueue_step(b, 0.f, false);
+        if (rc) return rc;
+        int32_t h[TC_COUNT];
+        rc = read_tree_counts(b, h);
+        if (rc) return rc;
+        const size_t ni = (size_t)h[TC_NINT], nc = (size_t)h[TC_NINT] + (size_t)h[TC_NLEAF];
+        if (h[TC_OVERFLOW] == 0 && ni <= b->core->tree.int_cap && nc <= b->core->tree.cell_cap) {
+            // room for the tree to grow as the galaxies evolve
+            return reserve_tree(b, 2 * ni + 64, 2 * nc + 64);
+        }
+        gi = std::max(gi * 2, 2 * ni + 64);
+        gc = std::max(gc * 2, 2 * nc + 64);
+    }
+    return bfail(b, NB_ENOMEM, "could not size the batched octree");
+}
+
+int build_graph(nb_batch* b, float dt) {
+    nb_sim* c = b->core;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    const bool prof = c->prof.on;
+    c->prof.on = false;
+    const uint64_t l0 = c->prof.launches;
+    NB_BCUDA(b, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(b, dt, true);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->prof.on = prof;
+    b->graph_kernels = c->prof.launches - l0;
+    c->prof.launches = l0;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return bfail(b, NB_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, NB_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    b->graph_dt = dt;
+    b->graph_dirty = false;
+    return NB_OK;
+}
+
+int sync_check(nb_batch* b) {
+    int rc = nb_synchronize(b->core);
+    if (rc) return bfail(b, rc, nb_last_error(b->core));
+    if (b->n_bh > 0) {
+        int32_t h[TC_COUNT];
+        rc = read_tree_counts(b, h);
+        if (rc) return rc;
+        if (h[TC_OVERFLOW] != 0 || h[TC_HASHFAIL] != 0)
+            return bfail(b, NB_ENOMEM, "batched octree exceeded its capacity; commit again to resize");
+    }
+    return NB_OK;
+}
+
+const nb_batch::Gal* find(nb_batch* b, int32_t galaxy) {
+    if (galaxy < 0 || (size_t)galaxy >= b->gal.size()) return nullptr;
+    return &b->gal[(size_t)galaxy];
+}
+
+}  // namespace
+
+extern "C" {
+
+int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta, nb_batch** out) {
+    if (!base || !out) return NB_EINVAL;
+    *out = nullptr;
+    if (!(bh_theta > 0) || !std::isfinite(bh_theta) || bh_threshold < 2) return NB_EINVAL;
+    nb_params p = *base;
+    p.kind = NB_SIM_BARNES_HUT;
+    nb_sim* core = nullptr;
+    int rc = nb_create(&p, &core);
+    if (rc) return rc;
+    nb_batch* b = new (std::nothrow) nb_batch();
+    if (!b) {
+        nb_destroy(core);
+        return NB_ENOMEM;
+    }
+    b->base = p;
+    b->bh_threshold = bh_threshold;
+    b->bh_theta = bh_theta;
+    b->core = core;
+    if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        nb_batch_destroy(b);
+        return NB_ENOMEM;
+    }
+    *out = b;
+    return NB_OK;
+}
+
+int nb_batch_destroy(nb_batch* b) {
+    if (!b) return NB_EINVAL;
+    if (b->core) cudaSetDevice(b->core->dev);
+    if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->warps, b->cell_q1,
+                    b->cell_q2, b->cell_first, b->body_dgal, b->dgal, b->units, b->unit_comp, b->part, b->next_unit};
+    for (void* p : ptrs) cudaFree(p);
+    if (b->core) nb_destroy(b->core);
+    delete b;
+    return NB_OK;
+}
+
+const char* nb_batch_last_error(const nb_batch* b) { return b ? b->err.c_str() : "null handle"; }
+
+void* nb_batch_stream(nb_batch* b) { return b && b->core ? (void*)b->core->stream : nullptr; }
+
+int nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t n, int32_t* galaxy) {
+    if (!b || !pos_mass4 || !vel4 || n == 0) return NB_EINVAL;
+    if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
+    if (n > (1u << 24)) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
+    b->h_pos.emplace_back(pos_mass4, pos_mass4 + 4 * n);
+    b->h_vel.emplace_back(vel4, vel4 + 4 * n);
+    nb_batch::Gal g;
+    g.n = n;
+    g.bh = n >= b->bh_threshold;
+    b->gal.push_back(g);
+    if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
+    return NB_OK;
+}
+
+int nb_batch_commit(nb_batch* b) {
+    if (!b) return NB_EINVAL;
+    if (b->committed) return bfail(b, NB_EBADSTATE, "already committed");
+    if (b->gal.empty()) return bfail(b, NB_EINVAL, "no galaxies");
+    cudaSetDevice(b->core->dev);
+    // layout: Barnes-Hut galaxies packed first (slot order), then direct-sum
+    // galaxies padded to multiples of 256 bodies
+    size_t off = 0;
+    int slot = 0;
+    for (auto& g : b->gal)
+        if (g.bh) {
+            g.off = off;
+            g.idx = slot++;
+            g.n_pad = g.n;
+            off += g.n;
+        }
+    b->n_bh = off;
+    b->nslot = slot;
+    if (slot >= (1 << 21)) return bfail(b, NB_EINVAL, "too many Barnes-Hut galaxies");
+    off = pad_up(off, 256);
+    b->dir_begin = off;
+    int dgi = 0;
+    for (auto& g : b->gal)
+        if (!g.bh) {
+            g.off = off;
+            g.idx = dgi++;
+            g.n_pad = pad_up(g.n, 256);
+            off += g.n_pad;
+            b->direct_pairs += (uint64_t)g.n * (uint64_t)(g.n - 1);
+        }
+    b->ndgal = dgi;
+    b->n_total = off;
+    if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
+    std::vector<float> pos(4 * b->n_total, 0.f), vel(4 * b->n_total, 0.f);
+    std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
+    std::vector<int4> gal_range(b->nslot), warps;
+    b->n_real = 0;
+    for (size_t k = 0; k < b->gal.size(); ++k) {
+        const auto& g = b->gal[k];
+        std::memcpy(&pos[4 * g.off], b->h_pos[k].data(), 16 * g.n);
+        std::memcpy(&vel[4 * g.off], b->h_vel[k].data(), 16 * g.n);
+        b->n_real += g.n;
+        if (g.bh) {
+            for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
+            slot_start[g.idx] = (int)g.off;
+            gal_range[g.idx] = make_int4((int)g.off, (int)g.n, 0, 0);
+            for (size_t w = 0; w < g.n; w += 32)
+                warps.push_back(make_int4(g.idx, (int)(g.off + w), (int)std::min<size_t>(32, g.n - w), 0));
+        } else {
+            for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
+        }
+    }
+    int rc = nb_init_soa(b->core, pos.data(), vel.data(), b->n_total);
+    if (rc) return bfail(b, rc, nb_last_error(b->core));
+    NB_BCUDA(b, upload(&b->body_slot, body_slot));
+    NB_BCUDA(b, upload(&b->slot_start, slot_start));
+    NB_BCUDA(b, upload(&b->gal_range, gal_range));
+    NB_BCUDA(b, upload(&b->warps, warps));
+    NB_BCUDA(b, upload(&b->body_dgal, body_dgal));
+    b->nwarps = (int)warps.size();
+    if (b->nslot > 0) {
+        NB_BCUDA(b, cudaMalloc(&b->gal_box, b->nslot * sizeof(float4)));
+        NB_BCUDA(b, cudaMalloc(&b->gal_root, b->nslot * sizeof(int32_t)));
+    }
+    b->h_pos.clear();
+    b->h_vel.clear();
+    rc = plan_units(b);
+    if (rc) return rc;
+    rc = size_tree(b);
+    if (rc) return rc;
+    b->committed = true;
+    return sync_check(b);
+}
+
+int nb_batch_set_tuning(nb_batch* b, const nb_tuning* t) {
+    if (!b || !t) return NB_EINVAL;
+    if (!tuning_valid(*t)) return bfail(b, NB_EINVAL, "unsupported tuning");
+    b->tune = *t;
+    b->graph_dirty = true;
+    if (!b->committed) return NB_OK;
+    cudaSetDevice(b->core->dev);
+    return plan_units(b);
+}
+
+int nb_batch_get_tuning(nb_batch* b, nb_tuning* t) {
+    if (!b || !t) return NB_EINVAL;
+    *t = b->tune;
+    return NB_OK;
+}
+
+int nb_batch_step(nb_batch* b, float dt, int nsteps) {
+    if (!b) return NB_EINVAL;
+    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+    if (nsteps < 0 || !std::isfinite(dt)) return bfail(b, NB_EINVAL, "bad dt or nsteps");
+    cudaSetDevice(b->core->dev);
+    if (b->graph_dirty || !(b->graph_dt == dt) || !b->exec) {
+        int rc = build_graph(b, dt);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        NB_BCUDA(b, cudaGraphLaunch(b->exec, b->core->stream));
+        b->core->prof.launches += b->graph_kernels;
+    }
+    return sync_check(b);
+}
+
+int nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4) {
+    if (!b) return NB_EINVAL;
+    const nb_batch::Gal* g = find(b, galaxy);
+    if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
+    cudaSetDevice(b->core->dev);
+    nb_sim* c = b->core;
+    const size_t n = g->n;
+    std::vector<float4> v(n), vc(n);
+    if (pos_mass4) NB_BCUDA(b, cudaMemcpy(pos_mass4, c->pos + g->off, n * 16, cudaMemcpyDeviceToHost));
+    if (vel4) {
+        NB_BCUDA(b, cudaMemcpy(v.data(), c->vel + g->off, n * 16, cudaMemcpyDeviceToHost));
+        NB_BCUDA(b, cudaMemcpy(vc.data(), c->velc + g->off, n * 16, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; ++i) {
+            vel4[4 * i] = (float)((double)v[i].x - vc[i].x);
+            vel4[4 * i + 1] = (float)((double)v[i].y - vc[i].y);
+            vel4[4 * i + 2] = (float)((double)v[i].z - vc[i].z);
+            vel4[4 * i + 3] = 0.f;
+        }
+    }
+    return NB_OK;
+}
+
+int nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3) {
+    if (!b || !force3) return NB_EINVAL;
+    const nb_batch::Gal* g = find(b, galaxy);
+    if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
+    cudaSetDevice(b->core->dev);
+    int rc = enqueue_step(b, 0.f, false);
+    if (rc) return rc;
+    rc = sync_check(b);
+    if (rc) return rc;
+    nb_sim* c = b->core;
+    std::vector<float4> a(g->n), p(g->n);
+    NB_BCUDA(b, cudaMemcpy(a.data(), c->acc + g->off, g->n * 16, cudaMemcpyDeviceToHost));
+    NB_BCUDA(b, cudaMemcpy(p.data(), c->pos + g->off, g->n * 16, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < g->n; ++i) {
+        const double m = p[i].w;
+        force3[3 * i] = m * a[i].x;
+        force3[3 * i + 1] = m * a[i].y;
+        force3[3 * i + 2] = m * a[i].z;
+    }
+    return NB_OK;
+}
+
+int nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last) {
+    if (!b) return NB_EINVAL;
+    if (galaxies) *galaxies = b->gal.size();
+    if (bodies) *bodies = b->committed ? b->n_real : 0;
+    if (interactions_last) {
+        unsigned long long v = 0;
+        if (b->committed && b->n_bh > 0) {
+            cudaSetDevice(b->core->dev);
+            NB_BCUDA(b, cudaMemcpy(&v, b->core->tree.interactions, sizeof(v), cudaMemcpyDeviceToHost));
+        }
+        *interactions_last = (uint64_t)v + b->direct_pairs;
+    }
+    return NB_OK;
+}
+
+// Project autotuner: candidate leaf sizes for the Barnes-Hut members, then
+// candidate direct-sum tilings, each timed over trial_steps graph replays with
+// CUDA events; the state is restored after every trial.
+int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
+    if (!b) return NB_EINVAL;
+    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+    if (trial_steps < 1) return bfail(b, NB_EINVAL, "trial_steps >= 1");
+    cudaSetDevice(b->core->dev);
+    nb_sim* c = b->core;
+    const size_t bytes = c->n_pad * sizeof(float4);
+    float4* save = nullptr;
+    NB_BCUDA(b, cudaMalloc(&save, 4 * bytes));
+    auto snapshot = [&](bool restore) {
+        float4* arrs[4] = {c->pos, c->posc, c->vel, c->velc};
+        for (int k = 0; k < 4; ++k) {
+            if (restore) cudaMemcpyAsync(arrs[k], save + k * c->n_pad, bytes, cudaMemcpyDeviceToDevice, c->stream);
+            else cudaMemcpyAsync(save + k * c->n_pad, arrs[k], bytes, cudaMemcpyDeviceToDevice, c->stream);
+        }
+    };
+    snapshot(false);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto trial = [&](const nb_tuning& t, float* ms) -> int {
+        int rc = nb_batch_set_tuning(b, &t);
+        if (rc) return rc;
+        rc = build_graph(b, dt);
+        if (rc) return rc;
+        cudaGraphLaunch(b->exec, c->stream);   // warm-up
+        cudaEventRecord(e0, c->stream);
+        for (int k = 0; k < trial_steps; ++k) cudaGraphLaunch(b->exec, c->stream);
+        cudaEventRecord(e1, c->stream);
+        rc = sync_check(b);
+        if (rc) return rc;
+        cudaEventElapsedTime(ms, e0, e1);
+        snapshot(true);
+        return NB_OK;
+    };
+    nb_tuning best = b->tune;
+    float best_ms = INFINITY;
+    int rc = NB_OK;
+    const int leafs[] = {8, 16, 32, 64};
+    for (int ls : (b->n_bh > 0 ? std::vector<int>(leafs, leafs + 4) : std::vector<int>{best.leaf_size})) {
+        nb_tuning t = best;
+        t.leaf_size = ls;
+        float ms = 0.f;
+        rc = trial(t, &ms);
+        if (rc) break;
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    const int shapes[][3] = {{128, 1, 1024}, {128, 2, 1024}, {64, 1, 1024}, {128, 1, 2048}, {256, 1, 1024}, {128, 2, 2048}};
+    if (!rc && b->ndgal > 0) {
+        const nb_tuning base_t = best;
+        for (const auto& sh : shapes) {
+            nb_tuning t = base_t;
+            t.direct_block = sh[0];
+            t.direct_ipt = sh[1];
+            t.direct_jtile = sh[2];
+            float ms = 0.f;
+            rc = trial(t, &ms);
+            if (rc) break;
+            if (ms < best_ms) { best_ms = ms; best = t; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    snapshot(true);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(save);
+    if (rc) return rc;
+    return nb_batch_set_tuning(b, &best);
+}
+
+}  // extern "C"

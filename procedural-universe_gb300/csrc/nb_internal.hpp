@@ -90,6 +90,7 @@ enum : int {
     TC_GAPS = 3,      // bodies whose path met a gap between float child bounds
     TC_DEEPER = 4,    // depth-cap buckets whose bodies differ (the reference would split further)
     TC_HASHFAIL = 5,  // failed internal-node lookups (must stay 0)
+    TC_OVERFLOW = 6,  // nodes beyond the allocated capacity (must stay 0)
     TC_COUNT = 8
 };
 
@@ -174,6 +175,10 @@ cudaError_t tree_build(nb_sim* sim);
 cudaError_t tree_forces(nb_sim* sim);
 cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal);
 float theta_float(double theta);   // smallest float >= theta
+// Batched form: topology of pre-computed keys without host synchronisation.
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D);
+cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells);
+int tree_sort_tile();
 
 // ---- profiling (nb_api.cu) ----
 // Records CUDA events around one phase on sim->stream when profiling is on

@@ -154,7 +154,7 @@ int nb_tree_stats(nb_sim* s, int64_t* stats8) {
     stats8[4] = h[TC_DEEPER];
     stats8[5] = h[TC_HASHFAIL];
     stats8[6] = (int64_t)s->n - h[TC_NIN];
-    stats8[7] = 0;
+    stats8[7] = h[TC_OVERFLOW];
     return NB_OK;
 }
 

@@ -236,6 +236,7 @@ struct TopoView {
     const int32_t* vals;      // body index per sorted position
     const int32_t* depth;     // per body (input order)
     int n_in, n_total, D;
+    int int_cap, cell_cap;    // capacities of the internal-node and cell arrays
     __device__ int delta(int s) const {   // common levels of sorted bodies s and s+1; -1 past the end
         if (s < 0 || s + 1 >= n_in) return -1;
         int l = lcp_levels(keys[s], keys[s + 1], D);
@@ -369,6 +370,10 @@ __global__ void k_emit(TopoView tv, const int32_t* __restrict__ int_base, int32_
     const int base = int_base[s];
     for (int l = lo; l <= hi; ++l) {
         const int k = base + (l - lo);
+        if (k >= tv.int_cap) {
+            atomicAdd(&counters[TC_OVERFLOW], 1);
+            break;
+        }
         const uint64_t code = node_code(key, l, tv.D);
         int_level[k] = l;
         int_first[k] = s;
@@ -379,16 +384,22 @@ __global__ void k_emit(TopoView tv, const int32_t* __restrict__ int_base, int32_
 
 __global__ void k_link_internal(const int32_t* __restrict__ int_level, const int32_t* __restrict__ int_first,
                                 const uint64_t* __restrict__ int_code, TopoView tv, int n_int,
+                                const int32_t* __restrict__ n_int_dev,
                                 const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv, uint32_t hmask,
                                 int32_t* __restrict__ int_parent, uint32_t* __restrict__ int_mask,
                                 int32_t* __restrict__ int_nint, int32_t* __restrict__ counters) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_int || k == 0) return;
+    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+    if (k >= ni || k == 0) return;
     const int l = int_level[k];
     const int s = int_first[k];
     const uint64_t code = int_code[k];
     const int prev = (s > 0) ? tv.delta(s - 1) : -1;
     const int parent = (l > prev + 1) ? k - 1 : hash_find(hk, hv, hmask, code >> 3, counters);
+    if (parent < 0 || parent >= ni) {
+        atomicAdd(&counters[TC_OVERFLOW], 1);
+        return;
+    }
     int_parent[k] = parent;
     atomicOr(&int_mask[parent], 1u << (unsigned)(code & 7ull));
     atomicAdd(&int_nint[parent], 1);
@@ -406,13 +417,19 @@ __global__ void k_link_leaves(TopoView tv, const int32_t* __restrict__ int_base,
     tv.info(s, lo, hi, nint, lf2, cur);
     const uint64_t code = node_code(tv.keys[s], lf, tv.D);
     const int parent = nint > 0 ? int_base[s] + (lf - 1 - lo) : hash_find(hk, hv, hmask, code >> 3, counters);
+    if (parent < 0 || parent >= tv.int_cap) {
+        atomicAdd(&counters[TC_OVERFLOW], 1);
+        return;
+    }
     leaf_parent[s] = parent;
     atomicOr(&int_mask[parent], 1u << (unsigned)(code & 7ull));
 }
 
-__global__ void k_popc(const uint32_t* __restrict__ mask, int n_int, int32_t* __restrict__ out) {
+__global__ void k_popc(const uint32_t* __restrict__ mask, int n_int, const int32_t* __restrict__ n_int_dev,
+                       int32_t* __restrict__ out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n_int) out[k] = __popc(mask[k]);
+    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+    if (k < n_int) out[k] = k < ni ? __popc(mask[k]) : 0;
 }
 
 // Opening thresholds of a cell for the traversal: with r^2 computed exactly
@@ -432,15 +449,21 @@ __device__ __forceinline__ int child_cell(const int32_t* int_block, const uint32
 
 __global__ void k_place_internal(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
                                  const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
-                                 const int32_t* __restrict__ int_block, int n_int, float half, float theta_f,
+                                 const int32_t* __restrict__ int_block, int n_int,
+                                 const int32_t* __restrict__ n_int_dev, int cell_cap, float half, float theta_f,
                                  int32_t* __restrict__ int_cell, int4* __restrict__ cell_meta,
                                  float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
                                  uint64_t* __restrict__ cell_code) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_int) return;
+    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+    if (k >= ni) return;
     const uint64_t code = int_code[k];
     const int l = int_level[k];
     const int cell = (k == 0) ? 0 : child_cell(int_block, int_mask, int_parent[k], (int)(code & 7ull));
+    if (cell >= cell_cap) {
+        int_cell[k] = 0;
+        return;
+    }
     int_cell[k] = cell;
     float3 lo, hi;
     float side;
@@ -468,6 +491,7 @@ __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_lev
     if (lf < 0) return;
     const uint64_t code = node_code(tv.keys[s], lf, tv.D);
     const int cell = (lf == 0) ? 0 : child_cell(int_block, int_mask, leaf_parent[s], (int)(code & 7ull));
+    if (cell >= tv.cell_cap) return;
     float3 lo, hi;
     float side;
     node_bounds(code, lf, half, lo, hi, side);
@@ -538,13 +562,15 @@ __device__ void finish_node(int k, const int32_t* int_cell, const int32_t* int_b
     __stcg(&cell_count[c], count);
 }
 
-__global__ void k_mass(int n_int, const int32_t* __restrict__ int_parent, const int32_t* __restrict__ int_nint,
+__global__ void k_mass(int n_int, const int32_t* __restrict__ n_int_dev, const int32_t* __restrict__ int_parent,
+                       const int32_t* __restrict__ int_nint,
                        int32_t* __restrict__ int_pending, const int32_t* __restrict__ int_cell,
                        const int32_t* __restrict__ int_block, const uint32_t* __restrict__ int_mask,
                        float4* __restrict__ cell_com, double* __restrict__ cell_mass,
                        int32_t* __restrict__ cell_count, int dropped) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_int || int_nint[k] != 0) return;
+    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+    if (k >= ni || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {   // a path has at most 22 internal nodes
         finish_node(k, int_cell, int_block, int_mask, cell_com, cell_mass, cell_count, dropped);
         if (k == 0) return;
@@ -672,6 +698,8 @@ static TopoView topo_view(nb_sim* sim) {
     tv.n_in = t.n_in;
     tv.n_total = (int)sim->n;
     tv.D = sim->prm.max_depth;
+    tv.int_cap = (int)t.int_cap;
+    tv.cell_cap = (int)t.cell_cap;
     return tv;
 }
 
@@ -740,15 +768,16 @@ cudaError_t tree_build(nb_sim* sim) {
         const int nbk = (t.n_in + kEmitBlock - 1) / kEmitBlock;
         k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals,
                                           hmask, t.counters);
-        k_link_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, ni, t.hkeys,
+        k_link_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, ni, nullptr, t.hkeys,
                                                          t.hvals, hmask, t.int_parent, t.int_mask, t.int_nint,
                                                          t.counters);
         k_link_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask,
                                                  t.leaf_parent, t.int_mask, t.counters);
-        k_popc<<<(ni + 255) / 256, 256, 0, st>>>(t.int_mask, ni, t.int_block);
+        k_popc<<<(ni + 255) / 256, 256, 0, st>>>(t.int_mask, ni, nullptr, t.int_block);
         NB_TRY(exclusive_scan(t.int_block, t.int_block, ni, t.scan_sums, nullptr, st));
         k_place_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
-                                                          t.int_block, ni, sim->prm.bounds_half, tf, t.int_cell,
+                                                          t.int_block, ni, nullptr, (int)t.cell_cap, sim->prm.bounds_half,
+                                                          tf, t.int_cell,
                                                           t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
         k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask,
                                                   t.int_block, t.spos, sim->prm.bounds_half, tf, t.cell_com,
@@ -758,7 +787,7 @@ cudaError_t tree_build(nb_sim* sim) {
     }
     {
         PhaseScope ps(sim, NB_PHASE_MASS);
-        k_mass<<<(ni + 255) / 256, 256, 0, st>>>(ni, t.int_parent, t.int_nint, t.int_pending, t.int_cell,
+        k_mass<<<(ni + 255) / 256, 256, 0, st>>>(ni, nullptr, t.int_parent, t.int_nint, t.int_pending, t.int_cell,
                                                 t.int_block, t.int_mask, t.cell_com, t.cell_mass, t.cell_count,
                                                 n - t.n_in);
         NB_TRY(cudaGetLastError());
@@ -785,5 +814,103 @@ cudaError_t tree_keys_export(nb_sim* sim, uint64_t* d_keys, int32_t* d_depth) {
     sim->tree_valid = false;   // the sort buffers no longer match the tree
     return cudaSuccess;
 }
+
+}  // namespace nb
+
+// ----------------------------------------------------------------------------
+// Topology without host synchronisation, for the batched form (its steps are
+// captured in a CUDA graph).  The caller has written keys, depths and the
+// identity order of bodies [0, n) into keys[0] / depth / vals[0] (pad entries
+// up to the sort tile with key ~0) and reserved capacities; every body lies
+// inside its cube.  Grid sizes come from the capacities; the kernels read the
+// node counts on the device and report overflow in counters[TC_OVERFLOW].
+// ----------------------------------------------------------------------------
+namespace nb {
+
+__global__ void k_counters_init(int32_t* __restrict__ counters, int n_in) {
+    if (threadIdx.x < TC_COUNT) counters[threadIdx.x] = threadIdx.x == TC_NIN ? n_in : 0;
+}
+
+// Moves the sort result into buffer 0 when the device plan left it in buffer 1.
+__global__ void k_sort_finalize(uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1, int32_t* __restrict__ v0,
+                                const int32_t* __restrict__ v1, int n, const int32_t* __restrict__ plan) {
+    if (plan[16] == 0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        k0[i] = k1[i];
+        v0[i] = v1[i];
+    }
+}
+
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
+    TreeBuffers& t = sim->tree;
+    const size_t nk = pad_up(std::max<size_t>((size_t)n, 1), kSortTile);
+    const int ntiles = (int)(nk / kSortTile);
+    cudaStream_t st = sim->stream;
+    {
+        PhaseScope ps(sim, NB_PHASE_SORT, 3 + kPasses * 5);
+        NB_TRY(cudaMemsetAsync(t.ghist, 0, kPasses * 256 * 4, st));
+        k_sort_ghist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.ghist);
+        k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan);
+        for (int p = 0; p < kPasses; ++p) {
+            k_sort_hist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], ntiles, t.plan, p, t.hist);
+            NB_TRY(exclusive_scan(t.hist, t.hist, 256 * ntiles, t.scan_sums, nullptr, st, t.plan + p));
+            k_sort_scatter<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles,
+                                                            t.hist, t.plan, p);
+        }
+        k_sort_finalize<<<(n + 255) / 256, 256, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], n, t.plan);
+        NB_TRY(cudaGetLastError());
+    }
+    t.final_buf = 0;
+    t.n_in = n;
+    TopoView tv;
+    tv.keys = t.keys[0];
+    tv.vals = t.vals[0];
+    tv.depth = t.depth;
+    tv.n_in = n;
+    tv.n_total = n;
+    tv.D = D;
+    tv.int_cap = (int)t.int_cap;
+    tv.cell_cap = (int)t.cell_cap;
+    const int icap = (int)t.int_cap;
+    const uint32_t hmask = (uint32_t)(t.hash_cap - 1);
+    const int nbk = (n + kEmitBlock - 1) / kEmitBlock;
+    PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 12);
+    k_counters_init<<<1, 32, 0, st>>>(t.counters, n);
+    k_gather<<<(n + 255) / 256, 256, 0, st>>>(pos, t.vals[0], n, t.spos);
+    k_positions<<<(n + 255) / 256, 256, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters);
+    NB_TRY(exclusive_scan(t.pos_nint, t.pos_nint, n, t.scan_sums, t.counters + TC_NINT, st));
+    NB_TRY(cudaMemsetAsync(t.hkeys, 0, t.hash_cap * 8, st));
+    NB_TRY(cudaMemsetAsync(t.int_mask, 0, (size_t)icap * 4, st));
+    NB_TRY(cudaMemsetAsync(t.int_nint, 0, (size_t)icap * 4, st));
+    NB_TRY(cudaMemsetAsync(t.int_pending, 0, (size_t)icap * 4, st));
+    k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals, hmask,
+                                      t.counters);
+    k_link_internal<<<(icap + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, icap,
+                                                       t.counters + TC_NINT, t.hkeys, t.hvals, hmask, t.int_parent,
+                                                       t.int_mask, t.int_nint, t.counters);
+    k_link_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask, t.leaf_parent,
+                                             t.int_mask, t.counters);
+    k_popc<<<(icap + 255) / 256, 256, 0, st>>>(t.int_mask, icap, t.counters + TC_NINT, t.int_block);
+    NB_TRY(exclusive_scan(t.int_block, t.int_block, icap, t.scan_sums, nullptr, st));
+    k_place_internal<<<(icap + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
+                                                        t.int_block, icap, t.counters + TC_NINT, (int)t.cell_cap,
+                                                        sim->prm.bounds_half, 1.0f, t.int_cell, t.cell_meta, t.cell_lo,
+                                                        t.cell_hi, t.cell_code);
+    k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask, t.int_block,
+                                              t.spos, sim->prm.bounds_half, 1.0f, t.cell_com, t.cell_mass,
+                                              t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+    return cudaGetLastError();
+}
+
+// Capacity of the node arrays for a batched build: exact counts are measured
+// once with a synchronising build and doubled (positions evolve).
+cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells) {
+    NB_TRY(reserve_bodies(sim, pad_up(std::max<size_t>((size_t)n, 1), kSortTile)));
+    NB_TRY(reserve_scan(sim, std::max((size_t)sim->tree.body_cap, (size_t)256 * (sim->tree.body_cap / kSortTile))));
+    return reserve_nodes(sim, n_int, n_cells);
+}
+
+int tree_sort_tile() { return kSortTile; }
 
 }  // namespace nb

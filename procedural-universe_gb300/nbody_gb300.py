@@ -343,3 +343,126 @@ class NBodySim:
         c = None if colour is None else np.ascontiguousarray(colour, np.float32)
         self._check(lib().nb_render_vertices(self._h, _ptr(c), scale, _ptr(out), self.n), "nb_render_vertices")
         return out
+
+
+class nb_tuning(ctypes.Structure):
+    _fields_ = [("direct_block", ctypes.c_int), ("direct_ipt", ctypes.c_int), ("direct_jtile", ctypes.c_int),
+                ("leaf_size", ctypes.c_int), ("traverse_block", ctypes.c_int)]
+
+
+def _bind_batch():
+    L = lib()
+    if getattr(L, "_batch_bound", False):
+        return L
+    vp, sz, i32, f32, f64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_float, ctypes.c_double
+    sig = {
+        "nb_batch_create": ([vp, sz, f64, vp], i32),
+        "nb_batch_destroy": ([vp], i32),
+        "nb_batch_last_error": ([vp], ctypes.c_char_p),
+        "nb_batch_add": ([vp, vp, vp, sz, vp], i32),
+        "nb_batch_commit": ([vp], i32),
+        "nb_batch_set_tuning": ([vp, vp], i32),
+        "nb_batch_get_tuning": ([vp, vp], i32),
+        "nb_batch_autotune": ([vp, f32, i32], i32),
+        "nb_batch_step": ([vp, f32, i32], i32),
+        "nb_batch_read": ([vp, i32, vp, vp], i32),
+        "nb_batch_forces": ([vp, i32, vp], i32),
+        "nb_batch_info": ([vp, vp, vp, vp], i32),
+        "nb_batch_stream": ([vp], vp),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    L._batch_bound = True
+    return L
+
+
+class NBodyBatch:
+    """Batched form: many galaxies stepped together (nb_batch*)."""
+
+    def __init__(self, bh_threshold=8192, bh_theta=0.6, **params):
+        L = _bind_batch()
+        self._h = ctypes.c_void_p()
+        p = default_params(**params)
+        rc = L.nb_batch_create(ctypes.byref(p), bh_threshold, bh_theta, ctypes.byref(self._h))
+        if rc:
+            raise NBodyError(rc, "nb_batch_create failed")
+        self.sizes = []
+
+    def _check(self, rc, what):
+        if rc:
+            msg = lib().nb_batch_last_error(self._h)
+            raise NBodyError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if self._h:
+            lib().nb_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return lib().nb_batch_stream(self._h) or 0
+
+    def add(self, pos_mass, vel) -> int:
+        pm = np.ascontiguousarray(pos_mass, np.float32)
+        v = np.ascontiguousarray(vel, np.float32)
+        g = ctypes.c_int32(-1)
+        self._check(lib().nb_batch_add(self._h, _ptr(pm), _ptr(v), pm.shape[0], ctypes.byref(g)), "nb_batch_add")
+        self.sizes.append(pm.shape[0])
+        return g.value
+
+    def commit(self):
+        self._check(lib().nb_batch_commit(self._h), "nb_batch_commit")
+
+    def step(self, dt, nsteps=1):
+        self._check(lib().nb_batch_step(self._h, dt, nsteps), "nb_batch_step")
+
+    def autotune(self, dt, trial_steps=3):
+        self._check(lib().nb_batch_autotune(self._h, dt, trial_steps), "nb_batch_autotune")
+
+    def tuning(self) -> dict:
+        t = nb_tuning()
+        self._check(lib().nb_batch_get_tuning(self._h, ctypes.byref(t)), "nb_batch_get_tuning")
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def set_tuning(self, **kw):
+        t = nb_tuning()
+        self._check(lib().nb_batch_get_tuning(self._h, ctypes.byref(t)), "nb_batch_get_tuning")
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(lib().nb_batch_set_tuning(self._h, ctypes.byref(t)), "nb_batch_set_tuning")
+
+    def read(self, g):
+        n = self.sizes[g]
+        pm = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 4), np.float32)
+        self._check(lib().nb_batch_read(self._h, g, _ptr(pm), _ptr(v)), "nb_batch_read")
+        return pm, v
+
+    def forces(self, g):
+        f = np.zeros((self.sizes[g], 3), np.float64)
+        self._check(lib().nb_batch_forces(self._h, g, _ptr(f)), "nb_batch_forces")
+        return f
+
+    def info(self):
+        ng, nb_, it = ctypes.c_size_t(0), ctypes.c_size_t(0), ctypes.c_uint64(0)
+        self._check(lib().nb_batch_info(self._h, ctypes.byref(ng), ctypes.byref(nb_), ctypes.byref(it)),
+                    "nb_batch_info")
+        return dict(galaxies=ng.value, bodies=nb_.value, interactions=it.value)
