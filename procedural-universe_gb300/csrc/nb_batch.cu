@@ -155,8 +155,8 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
     const float S = (float)b->base.softening2;
     const float G = (float)b->base.G;
     TreeBuffers& t = c->tree;
-    NB_BCUDA(b, cudaMemsetAsync(t.interactions, 0, sizeof(unsigned long long), st));
     if (b->n_bh > 0) {
+        NB_BCUDA(b, cudaMemsetAsync(t.interactions, 0, sizeof(unsigned long long), st));
         const int n = (int)b->n_bh;
         const size_t nk = pad_up((size_t)n, (size_t)tree_sort_tile());
         {
