@@ -362,13 +362,22 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bh1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="bh1m", choices=sorted(WORKLOADS) + ["batch512", "served"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     import nb_build
     nb_build.build()
+    if args.workload in ("batch512", "served"):
+        import torch
+        import nbody_gb300 as nb
+        import bench_forms
+        if dist_env()[1] != 0:
+            return 0
+        fn = bench_forms.run_batch if args.workload == "batch512" else bench_forms.run_served
+        print(json.dumps(fn(args, nb, torch)))
+        return 0
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, w)

@@ -1,0 +1,155 @@
+"""Batched and served forms of the N-body step, measured for bench.py.
+
+batch512: 512 independent galaxies, particle counts log-uniform in
+[256, 65,536], each a Plummer sphere or an exponential disk (coin flip) from
+its own seed; Barnes-Hut (group opening test, theta=0.6, quadrupoles) for
+n >= 8192, direct sum below; eps=0.01, dt=1e-3.  One launch per phase, the
+step replayed from a CUDA graph, tiles and leaf size from the autotuner.
+Compared with sequential plain-path launches (one handle per galaxy, the
+reference's per-body Barnes-Hut at the same theta, or direct sum) on the
+same GPU, and with the CPU restatement of the reference on a 16-galaxy
+sample.
+
+served: Poisson arrivals (seeded) of galaxy-generation jobs, n log-uniform in
+[1,024, 1,048,576], disk + bulge as in the 1M-body workload, 200 steps each,
+Barnes-Hut theta=0.5, admitted against a 120 GB device-memory budget and
+stepped together by continuous batching (see nb_server_* in the C-ABI).
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+
+METRIC = "body-steps/s"
+
+
+def batch_galaxies(nb, seed=2024, count=512, lo=256, hi=65536):
+    rng = np.random.default_rng(seed)
+    ns = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(int)
+    models = rng.integers(0, 2, count)
+    gals = []
+    for k, (n, m) in enumerate(zip(ns, models)):
+        if m == 0:
+            gals.append(nb.seed_plummer(seed * 1000 + k, int(n)))
+        else:
+            gals.append(nb.seed_disk(seed * 1000 + k, int(n), bulge_frac=0.0))
+    return gals
+
+
+def sequential_plain(nb, gals, eps2, dt, theta, threshold, steps=2):
+    """Body-steps/s of stepping every galaxy with its own plain handle, one after another."""
+    total_t = 0.0
+    total_n = 0
+    for pm, v in gals:
+        n = pm.shape[0]
+        kind = nb.SIM_BARNES_HUT if n >= threshold else nb.SIM_BRUTE_FORCE
+        with nb.NBodySim(kind=kind, softening2=eps2, theta=theta) as s:
+            s.init_soa(pm, v)
+            s.step(dt, 1)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(dt, steps)
+            s.synchronize()
+            total_t += (time.perf_counter() - t0) / steps
+        total_n += n
+    return total_n / total_t
+
+
+def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7):
+    """The reference's CPU algorithms (oracle restatement) on a galaxy sample."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(gals), min(count, len(gals)), replace=False)
+    t_tot = 0.0
+    n_tot = 0
+    for g in pick:
+        pm, v = gals[g]
+        rec = O.particles_from_soa(pm, v)
+        t0 = time.perf_counter()
+        if pm.shape[0] >= threshold:
+            tree = O.OracleTree(rec)
+            tree.forces(G=1.0, S=eps2, theta=theta)
+            tree.close()
+        else:
+            O.direct_forces(rec, G=1.0, S=eps2)
+        t_tot += time.perf_counter() - t0
+        n_tot += pm.shape[0]
+    return {"value": n_tot / t_tot, "unit": METRIC, "cores": O.default_threads() + 1, "kind": "port",
+            "sample": "%d of the galaxies (%d bodies), one force pass each (Barnes-Hut per-body rule at theta=%.1f "
+                      "for n >= %d, direct sum below) on all host cores" % (len(pick), n_tot, theta, threshold)}
+
+
+def run_batch(args, nb, torch):
+    eps2, dt, theta, threshold = 1e-4, 1e-3, 0.6, 8192
+    gals = batch_galaxies(nb)
+    n_real = sum(pm.shape[0] for pm, _ in gals)
+    stream = torch.cuda.Stream()
+    b = nb.NBodyBatch(bh_threshold=threshold, bh_theta=theta, softening2=eps2, stream=stream.cuda_stream)
+    for pm, v in gals:
+        b.add(pm, v)
+    t0 = time.perf_counter()
+    b.commit()
+    t_commit = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.autotune(dt, 2)
+    t_tune = time.perf_counter() - t0
+    b.step(dt, args.warmup)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        evs[k][0].record(stream)
+        b.step(dt, 1)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(sum(a.elapsed_time(c) for a, c in evs))
+    value = n_real * args.steps / (ms * 1e-3)
+    info = b.info()
+    # end to end: whole-batch state from pinned host memory, step, positions back
+    pin_pos = torch.empty((n_real, 4), dtype=torch.float32, pin_memory=True)
+    pin_vel = torch.empty((n_real, 4), dtype=torch.float32, pin_memory=True)
+    hp = pin_pos.numpy()
+    hv = pin_vel.numpy()
+    b.read_state(hp, hv)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b.write_state(hp, hv)
+        b.step(dt, 1)
+        b.read_state(hp, None)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    # force error of the Barnes-Hut members vs the FP64 direct sum
+    errs = []
+    bh_ids = [g for g, (pm, _) in enumerate(gals) if pm.shape[0] >= threshold]
+    for g in bh_ids[:8]:
+        pm, v = gals[g]
+        cur_pm, cur_v = b.read(g)
+        F = b.forces(g)
+        t = np.arange(0, pm.shape[0], max(1, pm.shape[0] // 1024)).astype(np.int32)
+        with nb.NBodySim(kind=nb.SIM_BRUTE_FORCE, softening2=eps2) as s:
+            s.init_soa(cur_pm, cur_v)
+            F64 = s.fp64_forces(t)
+        errs.append(float(np.linalg.norm(F[t] - F64) / np.linalg.norm(F64)))
+    tune = b.tuning()
+    b.close()
+    seq = sequential_plain(nb, gals, eps2, dt, theta, threshold)
+    cpu = None if args.no_cpu_baseline else cpu_sample(gals, eps2, theta, threshold)
+    return {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies)",
+        "config": {"workload": "batch512", "galaxies": len(gals), "bodies": n_real,
+                   "barnes_hut_members": len(bh_ids), "theta": theta, "eps": 0.01, "dt": dt,
+                   "l2": "inputs (%.0f MB of state) larger than L2" % (n_real * 64 / 1e6)},
+        "sequential_plain": {"value": seq, "unit": METRIC,
+                             "how": "one plain handle per galaxy, stepped one galaxy after another (2 steps each)"},
+        "speedup_vs_sequential_plain": value / seq,
+        "force_rel_l2_vs_fp64_max": max(errs) if errs else None, "force_err_galaxies": len(errs),
+        "interactions_per_step": info["interactions"], "tuning": tune,
+        "e2e": {"value": n_real * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": n_real * 32,
+                "d2h_bytes_per_step": n_real * 16, "steps": e2e_steps},
+        "cpu_baseline": cpu, "setup_s": {"commit": t_commit, "autotune": t_tune},
+    }

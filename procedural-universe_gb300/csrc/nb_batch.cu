@@ -608,3 +608,44 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
 }
 
 }  // extern "C"
+
+// ---- whole-batch state transfer (the reference-facing end-to-end path) -----
+extern "C" {
+
+// Uploads the state of every galaxy (galaxies in index order, concatenated:
+// n_bodies x float4 each) from host buffers; the tree and graph are reused.
+int nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4) {
+    if (!b || !pos_mass4 || !vel4) return NB_EINVAL;
+    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+    cudaSetDevice(b->core->dev);
+    nb_sim* c = b->core;
+    size_t src = 0;
+    for (const auto& g : b->gal) {
+        NB_BCUDA(b, cudaMemcpyAsync(c->pos + g.off, pos_mass4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
+        NB_BCUDA(b, cudaMemcpyAsync(c->vel + g.off, vel4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
+        NB_BCUDA(b, cudaMemsetAsync(c->posc + g.off, 0, g.n * 16, c->stream));
+        NB_BCUDA(b, cudaMemsetAsync(c->velc + g.off, 0, g.n * 16, c->stream));
+        src += g.n;
+    }
+    return NB_OK;
+}
+
+// Downloads positions+masses (and, if vel4 is not NULL, velocities) of every
+// galaxy into host buffers in the same concatenated order.
+int nb_batch_read_state(nb_batch* b, float* pos_mass4, float* vel4) {
+    if (!b || !pos_mass4) return NB_EINVAL;
+    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+    cudaSetDevice(b->core->dev);
+    nb_sim* c = b->core;
+    size_t dst = 0;
+    for (const auto& g : b->gal) {
+        NB_BCUDA(b, cudaMemcpyAsync(pos_mass4 + 4 * dst, c->pos + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
+        if (vel4)
+            NB_BCUDA(b, cudaMemcpyAsync(vel4 + 4 * dst, c->vel + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
+        dst += g.n;
+    }
+    NB_BCUDA(b, cudaStreamSynchronize(c->stream));
+    return NB_OK;
+}
+
+}  // extern "C"

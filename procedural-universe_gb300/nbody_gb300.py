@@ -369,6 +369,8 @@ def _bind_batch():
         "nb_batch_forces": ([vp, i32, vp], i32),
         "nb_batch_info": ([vp, vp, vp, vp], i32),
         "nb_batch_stream": ([vp], vp),
+        "nb_batch_write_state": ([vp, vp, vp], i32),
+        "nb_batch_read_state": ([vp, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -460,6 +462,13 @@ class NBodyBatch:
         f = np.zeros((self.sizes[g], 3), np.float64)
         self._check(lib().nb_batch_forces(self._h, g, _ptr(f)), "nb_batch_forces")
         return f
+
+    def write_state(self, pos_mass, vel):
+        """Uploads every galaxy's state (concatenated in galaxy order)."""
+        self._check(lib().nb_batch_write_state(self._h, _ptr(pos_mass), _ptr(vel)), "nb_batch_write_state")
+
+    def read_state(self, pos_mass, vel=None):
+        self._check(lib().nb_batch_read_state(self._h, _ptr(pos_mass), _ptr(vel)), "nb_batch_read_state")
 
     def info(self):
         ng, nb_, it = ctypes.c_size_t(0), ctypes.c_size_t(0), ctypes.c_uint64(0)
