@@ -172,9 +172,10 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
             k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
                 (int)t.int_cap, t.counters + TC_NINT, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
                 t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_first,
-                t.cell_meta);
+                t.cell_meta, (int)t.cell_cap, n, c->d_err);
             k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
-                                                                 t.int_cell, t.counters + TC_NINT, b->gal_root,
+                                                                 t.int_cell, t.counters + TC_NINT, (int)t.int_cap,
+                                                                 b->gal_root,
                                                                  c->d_err);
         }
         {
@@ -185,7 +186,7 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
     k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(b->warps, b->nwarps, t.spos, t.vals[0], t.cell_com,      \
                                                         t.cell_meta, b->cell_q1, b->cell_q2, b->cell_first,      \
                                                         t.cell_count, t.cell_hi, b->gal_box, b->gal_root,        \
-                                                        (int)t.cell_cap, (int)t.int_cap, b->tune.leaf_size,      \
+                                                        (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size,   \
                                                         th * th, S, G, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
             else NB_GT(NB_LAW_REFERENCE);

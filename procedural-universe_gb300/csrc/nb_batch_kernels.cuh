@@ -122,10 +122,15 @@ __device__ void bucket_moments(const float4* spos, int first, int count, float4&
 
 __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* int_block, const uint32_t* int_mask,
                                const int32_t* int_first, const float4* spos, float4* cell_com, float4* cell_q1,
-                               float4* cell_q2, int32_t* cell_count, int32_t* cell_first, const int4* cell_meta) {
+                               float4* cell_q2, int32_t* cell_count, int32_t* cell_first, const int4* cell_meta,
+                               int cell_cap, int nbodies, int* err) {
     const int c = int_cell[k];
     const int F = 1 + int_block[k];
     const int nch = __popc(int_mask[k]);
+    if (c < 0 || c >= cell_cap || F + nch > cell_cap) {   // corrupt node: report, never dereference
+        record_error(err, DEV_TREE_OVERFLOW);
+        return;
+    }
     float4 ccm[8], cq1[8], cq2[8];
     float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     int count = 0;
@@ -139,6 +144,11 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
             cq1[j] = __ldcg(&cell_q1[ch]);
             cq2[j] = __ldcg(&cell_q2[ch]);
         } else if (kind == BK_BUCKET) {
+            if (mt.x < 0 || cnt < 0 || mt.x + cnt > nbodies) {
+                record_error(err, DEV_TREE_OVERFLOW);
+                ccm[j] = cq1[j] = cq2[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                continue;
+            }
             bucket_moments(spos, mt.x, cnt, ccm[j], cq1[j], cq2[j]);
         } else {
             ccm[j] = __ldcg(&cell_com[ch]);
@@ -175,13 +185,14 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_d
                                 const int32_t* __restrict__ int_first, const float4* __restrict__ spos,
                                 float4* __restrict__ cell_com, float4* __restrict__ cell_q1,
                                 float4* __restrict__ cell_q2, int32_t* __restrict__ cell_count,
-                                int32_t* __restrict__ cell_first, const int4* __restrict__ cell_meta) {
+                                int32_t* __restrict__ cell_first, const int4* __restrict__ cell_meta, int cell_cap,
+                                int nbodies, int* __restrict__ err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int ni = min(*n_int_dev, int_cap);
     if (k >= ni || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {
         finish_moments(k, int_cell, int_block, int_mask, int_first, spos, cell_com, cell_q1, cell_q2, cell_count,
-                       cell_first, cell_meta);
+                       cell_first, cell_meta, cell_cap, nbodies, err);
         if (k == 0) return;
         __threadfence();
         const int p = int_parent[k];
@@ -197,7 +208,7 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_d
 // galaxy's first sorted position.
 __global__ void k_batch_roots(const int32_t* __restrict__ slot_start, int nslot, const uint64_t* __restrict__ keys,
                               const int32_t* __restrict__ int_base, const int32_t* __restrict__ int_cell,
-                              const int32_t* __restrict__ n_int_dev, int32_t* __restrict__ root,
+                              const int32_t* __restrict__ n_int_dev, int int_cap, int32_t* __restrict__ root,
                               int32_t* __restrict__ err) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nslot) return;
@@ -208,7 +219,7 @@ __global__ void k_batch_roots(const int32_t* __restrict__ slot_start, int nslot,
         prev = x == 0 ? kBatchDepth : (__clzll((long long)x) - (64 - 3 * kBatchDepth)) / 3;
     }
     const int k = int_base[s] + (kSlotLevels - (prev + 1));
-    if (prev + 1 > kSlotLevels || k < 0 || k >= *n_int_dev) {
+    if (prev + 1 > kSlotLevels || k < 0 || k >= min(*n_int_dev, int_cap)) {
         root[g] = -1;
         record_error(err, DEV_TREE_OVERFLOW);
         return;
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
     const float4* __restrict__ cell_com, const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1,
     const float4* __restrict__ cell_q2, const int32_t* __restrict__ cell_first, const int32_t* __restrict__ cell_count,
     const float4* __restrict__ cell_hi, const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root,
-    int n_cells, int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
+    int n_cells, int nbodies, int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
     __shared__ float4 lcm[kGWarps][kGCells], lq1[kGWarps][kGCells], lq2[kGWarps][kGCells];
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
         const int4 pm = __ldg(&cell_meta[c]);
         const int F = pm.x, nch = (pm.w >> 4) & 15;
         if ((pm.w & 15) != BK_INTERNAL || F < 1 || nch > 8 || F + nch > n_cells) { bad = true; break; }
-        bool a_cell = false, a_range = false, a_push = false;
+        bool a_cell = false, a_range = false, a_push = false, a_bad = false;
         float4 ccm = make_float4(0.f, 0.f, 0.f, 0.f);
         int first = 0, count = 0, ch = 0;
         if (lane < nch) {
@@ -359,7 +370,10 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
             a_cell = accept && count > 2 && kind == BK_INTERNAL;
             a_range = !a_cell && (count <= leaf_size || kind != BK_INTERNAL);
             a_push = !a_cell && !a_range;
+            // node data outside the body range would be a corrupt tree: report, never dereference
+            if (a_range && (first < 0 || count < 0 || first + count > nbodies)) a_range = false, a_bad = true;
         }
+        if (__any_sync(0xffffffffu, a_bad)) { bad = true; break; }
         const uint32_t bc = __ballot_sync(0xffffffffu, a_cell);
         if (bc) {
             if (ncl + __popc(bc) > kGCells) flush_cells();

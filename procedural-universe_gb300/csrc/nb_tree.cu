@@ -490,6 +490,7 @@ __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_lev
     const int lf = leaf_level[s];
     if (lf < 0) return;
     const uint64_t code = node_code(tv.keys[s], lf, tv.D);
+    if (lf > 0 && (leaf_parent[s] < 0 || leaf_parent[s] >= tv.int_cap)) return;   // parent lost to an overflow
     const int cell = (lf == 0) ? 0 : child_cell(int_block, int_mask, leaf_parent[s], (int)(code & 7ull));
     if (cell >= tv.cell_cap) return;
     float3 lo, hi;
@@ -662,7 +663,8 @@ static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
         NB_TRY(grow((void**)&t.cell_code, cap * 8));
         t.cell_cap = cap;
     }
-    return reserve_scan(sim, std::max(n_int, (size_t)1));
+    // the batched build scans the whole internal-node capacity
+    return reserve_scan(sim, std::max(t.int_cap, (size_t)1));
 }
 
 cudaError_t tree_reserve(nb_sim* sim) {
