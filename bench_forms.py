@@ -81,6 +81,76 @@ def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7):
                       "for n >= %d, direct sum below) on all host cores" % (len(pick), n_tot, theta, threshold)}
 
 
+def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
+    import nbody_serve as ns
+    rng = np.random.default_rng(5)
+    gaps = rng.exponential(1.0 / rate, requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sizes = np.round(np.exp(rng.uniform(np.log(1024), np.log(1 << 20), requests))).astype(int)
+    server = ns.NBodyServer(max_active=64, steps_per_round=25, bh_threshold=1024, softening2=eps * eps, theta=theta)
+    ids = []
+    submitted = 0
+    t0 = server.clock()
+    while True:
+        now = server.clock() - t0
+        while submitted < requests and arrivals[submitted] <= now:
+            ids.append(server.submit(10_000 + submitted, int(sizes[submitted]), steps, dt, 0))
+            submitted += 1
+        a, q = server.tick()
+        if submitted == requests and a == 0 and q == 0:
+            break
+        if a == 0 and q == 0:
+            time.sleep(max(0.0, arrivals[submitted] - (server.clock() - t0)))
+    st = [server.status(i) for i in ids]
+    lat = np.array([s["done_s"] - s["submit_s"] for s in st])
+    makespan = max(s["done_s"] for s in st) - min(s["submit_s"] for s in st)
+    total = float(sizes.sum()) * steps
+    stats = server.stats()
+    server.close()
+    # sequential plain path: one handle per job (reference per-body Barnes-Hut), FIFO
+    service = []
+    for k, n in enumerate(sizes):
+        t0 = time.perf_counter()
+        pm, v = nb.seed_disk(10_000 + k, int(n))
+        t_gen = time.perf_counter() - t0
+        with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps * eps, theta=theta) as s:
+            s.init_soa(pm, v)
+            s.step(dt, 1)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.step(dt, 2)
+            s.synchronize()
+            t_step = (time.perf_counter() - t0) / 2
+        service.append(t_gen + steps * t_step)
+    service = np.array(service)
+    done, t = [], 0.0
+    for arr, sv in zip(arrivals, service):
+        t = max(t, arr) + sv
+        done.append(t)
+    seq_lat = np.array(done) - arrivals
+    seq_value = total / (done[-1] - arrivals[0])
+    return {
+        "metric": METRIC, "value": total / makespan, "unit": METRIC, "n_gpus": 1, "steps": steps,
+        "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies, Poisson arrivals)",
+        "config": {"workload": "served", "requests": requests, "rate_per_s": rate, "n_range": [1024, 1 << 20],
+                   "mean_n": float(sizes.mean()), "steps_per_job": steps, "theta": theta, "eps": eps, "dt": dt,
+                   "memory_budget_gb": 120, "max_active": 64, "steps_per_round": 25},
+        "offered": {"value": rate * float(sizes.mean()) * steps, "unit": METRIC},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "max": float(lat.max())},
+        "makespan_s": makespan, "rounds": stats["rounds"],
+        "sequential_plain": {"value": seq_value, "unit": METRIC,
+                             "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
+                                           "p99": float(np.percentile(seq_lat, 99))},
+                             "how": "each job generated then stepped by its own plain Barnes-Hut handle, FIFO, "
+                                    "the same arrivals; step time measured over 2 steps and scaled to %d" % steps},
+        "speedup_vs_sequential_plain": (total / makespan) / seq_value,
+        "cpu_baseline": None,
+        "cpu_baseline_note": "not timed for the served stream (hours of CPU work); see the bh1m workload",
+    }
+
+
 def run_batch(args, nb, torch):
     eps2, dt, theta, threshold = 1e-4, 1e-3, 0.6, 8192
     gals = batch_galaxies(nb)

@@ -272,6 +272,54 @@ int  nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4
 int  nb_batch_read_state(nb_batch* b, float* pos_mass4, float* vel4);
 void* nb_batch_stream(nb_batch* b);
 
+/* ---- served form: continuous batching of galaxy jobs ---------------------- */
+/* Jobs arrive, wait in a FIFO queue, are admitted while the estimated device
+ * bytes of the active jobs (about 170 bytes per body: state, tree, scratch)
+ * stay within memory_budget and a slot is free, and are stepped together in
+ * rounds by the batched form; a round takes at most steps_per_round steps and
+ * never more than the nearest job completion, so that finished jobs leave and
+ * queued ones enter between rounds.  A job keeps its state on the device for
+ * its whole life (moved device to device when the batch is rebuilt), so its
+ * result does not depend on the jobs it shared rounds with. */
+typedef struct nb_server nb_server;
+typedef struct nb_server_params {
+    nb_params base;           /* law, G, softening2, theta (Barnes-Hut), device     */
+    size_t   memory_budget;   /* bytes of device memory the active jobs may hold    */
+    int      max_active;      /* slots: jobs stepped together                       */
+    int      steps_per_round; /* steps per scheduling round                         */
+    size_t   bh_threshold;    /* n >= this: Barnes-Hut, else direct sum             */
+} nb_server_params;
+typedef struct nb_job {
+    uint64_t seed;
+    size_t   n;
+    int      steps;
+    float    dt;              /* jobs are stepped in rounds with the dt of the active jobs */
+    int      model;           /* 0 disk + 10% bulge (nb_seed_disk defaults), 1 Plummer   */
+} nb_job;
+typedef struct nb_job_status {
+    uint64_t id;
+    int      state;           /* 0 queued, 1 active, 2 done, -1 rejected           */
+    int      steps_done;
+    double   submit_s, admit_s, done_s;  /* server clock, seconds                  */
+    size_t   bytes;           /* estimated device bytes while active               */
+} nb_job_status;
+int  nb_server_default_params(nb_server_params* p);
+int  nb_server_create(const nb_server_params* p, nb_server** out);
+int  nb_server_destroy(nb_server* s);
+const char* nb_server_last_error(const nb_server* s);
+/* Queues a job; its initial conditions are generated when it is admitted. */
+int  nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id);
+/* One scheduling round: retire finished jobs (final state kept on the host),
+ * admit queued jobs that fit the budget and the free slots, step the active
+ * jobs.  Returns the active and queued counts. */
+int  nb_server_tick(nb_server* s, int* active, int* queued);
+double nb_server_clock(nb_server* s);
+int  nb_server_status(nb_server* s, uint64_t id, nb_job_status* out);
+/* Copies a finished job's final state (n x float4 each) to the host. */
+int  nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, size_t n);
+/* Body-steps completed and rounds run since creation. */
+int  nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds);
+
 /* ---- allocation-free direct sum -------------------------------------------- */
 /* No counterpart in the reference.  For callers that must not allocate device
  * memory while they step: a render loop held to a fixed device-memory budget,

@@ -28,6 +28,7 @@ struct nb_batch {
         size_t off = 0;   // first body in the concatenated arrays
         int idx = -1;     // slot (Barnes-Hut) or direct-galaxy index
         size_t n_pad = 0;
+        const float4* dsrc[4] = {nullptr, nullptr, nullptr, nullptr};   // device source (pos, posc, vel, velc)
     };
     std::vector<Gal> gal;
     std::vector<std::vector<float>> h_pos, h_vel;
@@ -310,6 +311,44 @@ const nb_batch::Gal* find(nb_batch* b, int32_t galaxy) {
 
 }  // namespace
 
+// ---- device-side hand-over between batches (used by the served form) -------
+namespace nb {
+
+// Adds a galaxy whose state (position+mass, position compensation, velocity,
+// velocity compensation) lives in device memory, e.g. in another batch; the
+// source must stay valid until nb_batch_commit returns.
+int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
+                     size_t n, int32_t* galaxy) {
+    if (!b || !pos || !posc || !vel || !velc || n == 0) return NB_EINVAL;
+    if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
+    b->h_pos.emplace_back();
+    b->h_vel.emplace_back();
+    nb_batch::Gal g;
+    g.n = n;
+    g.bh = n >= b->bh_threshold;
+    g.dsrc[0] = pos; g.dsrc[1] = posc; g.dsrc[2] = vel; g.dsrc[3] = velc;
+    b->gal.push_back(g);
+    if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
+    return NB_OK;
+}
+
+// Device state of a committed galaxy.
+int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,
+                       const float4** velc, size_t* n) {
+    if (!b || !b->committed || galaxy < 0 || (size_t)galaxy >= b->gal.size()) return NB_EINVAL;
+    const auto& g = b->gal[(size_t)galaxy];
+    *pos = b->core->pos + g.off;
+    *posc = b->core->posc + g.off;
+    *vel = b->core->vel + g.off;
+    *velc = b->core->velc + g.off;
+    *n = g.n;
+    return NB_OK;
+}
+
+int batch_set_tuning_quiet(nb_batch* b, const nb_tuning& t) { return nb_batch_set_tuning(b, &t); }
+
+}  // namespace nb
+
 extern "C" {
 
 int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta, nb_batch** out) {
@@ -409,8 +448,10 @@ int nb_batch_commit(nb_batch* b) {
     b->n_real = 0;
     for (size_t k = 0; k < b->gal.size(); ++k) {
         const auto& g = b->gal[k];
-        std::memcpy(&pos[4 * g.off], b->h_pos[k].data(), 16 * g.n);
-        std::memcpy(&vel[4 * g.off], b->h_vel[k].data(), 16 * g.n);
+        if (!g.dsrc[0]) {
+            std::memcpy(&pos[4 * g.off], b->h_pos[k].data(), 16 * g.n);
+            std::memcpy(&vel[4 * g.off], b->h_vel[k].data(), 16 * g.n);
+        }
         b->n_real += g.n;
         if (g.bh) {
             for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
@@ -424,6 +465,14 @@ int nb_batch_commit(nb_batch* b) {
     }
     int rc = nb_init_soa(b->core, pos.data(), vel.data(), b->n_total);
     if (rc) return bfail(b, rc, nb_last_error(b->core));
+    // galaxies handed over from another batch keep their exact state, compensation included
+    for (const auto& g : b->gal) {
+        if (!g.dsrc[0]) continue;
+        float4* dst[4] = {b->core->pos, b->core->posc, b->core->vel, b->core->velc};
+        for (int a = 0; a < 4; ++a)
+            NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                        b->core->stream));
+    }
     NB_BCUDA(b, upload(&b->body_slot, body_slot));
     NB_BCUDA(b, upload(&b->slot_start, slot_start));
     NB_BCUDA(b, upload(&b->gal_range, gal_range));

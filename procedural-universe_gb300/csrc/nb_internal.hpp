@@ -180,6 +180,12 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D);
 cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells);
 int tree_sort_tile();
 
+// ---- batched form hand-over (nb_batch.cu), used by the served form ----
+int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
+                     size_t n, int32_t* galaxy);
+int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,
+                       const float4** velc, size_t* n);
+
 // ---- profiling (nb_api.cu) ----
 // Records CUDA events around one phase on sim->stream when profiling is on
 // and counts `launches` kernel launches in either case.

@@ -1,0 +1,271 @@
+// nb_serve.cu -- served form: a request loop of galaxy-generation jobs with
+// continuous batching.
+//
+// Jobs wait in a FIFO queue; between rounds finished jobs leave (their final
+// state is copied to the host) and queued jobs are admitted while a slot is
+// free and the estimated device bytes of the active jobs stay within the
+// budget.  When the active set changes, a new batch is built from the active
+// jobs -- continuing jobs hand their state over device to device, new jobs
+// bring freshly generated initial conditions -- and the active jobs are
+// stepped together by the batched form for up to steps_per_round steps,
+// never past the nearest completion.  Every job's state stays on the device
+// from admission to completion.
+#include "nb_common.cuh"
+#include "nb_internal.hpp"
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <string>
+#include <vector>
+
+using namespace nb;
+
+namespace {
+
+// Upper estimate of the batched form's device bytes per body: state and
+// compensation (96), sort and topology scratch (~110), tree cells at twice the
+// measured count with quadrupoles (~400), direct-sum partials.
+constexpr size_t kBytesPerBody = 640;
+
+struct Job {
+    nb_job spec{};
+    nb_job_status st{};
+    int galaxy = -1;                // index in the current batch
+    std::vector<float> init_pos, init_vel, res_pos, res_vel;
+};
+
+}  // namespace
+
+struct nb_server {
+    nb_server_params prm{};
+    std::string err;
+    std::chrono::steady_clock::time_point t0;
+    uint64_t next_id = 1;
+    std::map<uint64_t, Job> jobs;
+    std::deque<uint64_t> queue;
+    std::vector<uint64_t> active;   // in batch galaxy order
+    nb_batch* batch = nullptr;
+    size_t bytes_used = 0;
+    float dt = NAN;                 // dt of the active jobs
+    uint64_t body_steps = 0, rounds = 0;
+};
+
+namespace {
+
+int sfail(nb_server* s, int code, const std::string& msg) {
+    if (s) s->err = msg;
+    return code;
+}
+
+double now_s(const nb_server* s) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->t0).count();
+}
+
+size_t job_bytes(const nb_job& j) { return j.n * kBytesPerBody; }
+
+int generate(Job& j) {
+    const size_t n = j.spec.n;
+    j.init_pos.assign(4 * n, 0.f);
+    j.init_vel.assign(4 * n, 0.f);
+    if (j.spec.model == 1) return nb_seed_plummer(j.spec.seed, n, 1.0, 1.0, j.init_pos.data(), j.init_vel.data());
+    return nb_seed_disk(j.spec.seed, n, 1.0, 1.0, 0.1, 0.1, 0.2, 0.05, j.init_pos.data(), j.init_vel.data());
+}
+
+// Builds a batch of the active jobs; continuing jobs take their state from
+// the previous batch (device to device).
+int rebuild(nb_server* s) {
+    nb_batch* nb2 = nullptr;
+    int rc = nb_batch_create(&s->prm.base, s->prm.bh_threshold, s->prm.base.theta, &nb2);
+    if (rc) return sfail(s, rc, "nb_batch_create failed");
+    for (uint64_t id : s->active) {
+        Job& j = s->jobs[id];
+        int32_t g = -1;
+        if (j.galaxy >= 0 && s->batch) {
+            const float4 *p, *pc, *v, *vc;
+            size_t n = 0;
+            rc = batch_device_state(s->batch, j.galaxy, &p, &pc, &v, &vc, &n);
+            if (!rc) rc = batch_add_device(nb2, p, pc, v, vc, n, &g);
+        } else {
+            rc = nb_batch_add(nb2, j.init_pos.data(), j.init_vel.data(), j.spec.n, &g);
+        }
+        if (rc) {
+            std::string m = nb_batch_last_error(nb2);
+            nb_batch_destroy(nb2);
+            return sfail(s, rc, "batch add: " + m);
+        }
+        j.galaxy = g;
+    }
+    rc = nb_batch_commit(nb2);
+    if (rc) {
+        std::string m = nb_batch_last_error(nb2);
+        nb_batch_destroy(nb2);
+        return sfail(s, rc, "batch commit: " + m);
+    }
+    if (s->batch) nb_batch_destroy(s->batch);
+    s->batch = nb2;
+    for (uint64_t id : s->active) {
+        Job& j = s->jobs[id];
+        j.init_pos.clear();
+        j.init_pos.shrink_to_fit();
+        j.init_vel.clear();
+        j.init_vel.shrink_to_fit();
+    }
+    return NB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nb_server_default_params(nb_server_params* p) {
+    if (!p) return NB_EINVAL;
+    std::memset(p, 0, sizeof(*p));
+    nb_default_params(&p->base);
+    p->base.softening2 = 0.005 * 0.005;
+    p->base.theta = 0.5;
+    p->memory_budget = (size_t)120 << 30;
+    p->max_active = 64;
+    p->steps_per_round = 25;
+    p->bh_threshold = 1024;
+    return NB_OK;
+}
+
+int nb_server_create(const nb_server_params* p, nb_server** out) {
+    if (!p || !out) return NB_EINVAL;
+    *out = nullptr;
+    if (p->max_active < 1 || p->steps_per_round < 1 || p->memory_budget == 0 || p->bh_threshold < 2 ||
+        !(p->base.theta > 0))
+        return NB_EINVAL;
+    nb_server* s = new (std::nothrow) nb_server();
+    if (!s) return NB_ENOMEM;
+    s->prm = *p;
+    s->t0 = std::chrono::steady_clock::now();
+    *out = s;
+    return NB_OK;
+}
+
+int nb_server_destroy(nb_server* s) {
+    if (!s) return NB_EINVAL;
+    if (s->batch) nb_batch_destroy(s->batch);
+    delete s;
+    return NB_OK;
+}
+
+const char* nb_server_last_error(const nb_server* s) { return s ? s->err.c_str() : "null handle"; }
+
+double nb_server_clock(nb_server* s) { return s ? now_s(s) : 0.0; }
+
+int nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id) {
+    if (!s || !job) return NB_EINVAL;
+    if (job->n < 2 || job->steps < 1 || !(job->dt > 0) || (job->model != 0 && job->model != 1))
+        return sfail(s, NB_EINVAL, "bad job");
+    Job j;
+    j.spec = *job;
+    j.st.id = s->next_id++;
+    j.st.state = 0;
+    j.st.submit_s = now_s(s);
+    j.st.bytes = job_bytes(*job);
+    if (j.st.bytes > s->prm.memory_budget) j.st.state = -1;   // can never fit
+    const uint64_t jid = j.st.id;
+    const bool queued = j.st.state == 0;
+    s->jobs.emplace(jid, std::move(j));
+    if (queued) s->queue.push_back(jid);
+    if (id) *id = jid;
+    return NB_OK;
+}
+
+int nb_server_tick(nb_server* s, int* active, int* queued) {
+    if (!s) return NB_EINVAL;
+    bool changed = false;
+    // retire finished jobs
+    std::vector<uint64_t> keep;
+    for (uint64_t id : s->active) {
+        Job& j = s->jobs[id];
+        if (j.st.steps_done >= j.spec.steps) {
+            j.res_pos.assign(4 * j.spec.n, 0.f);
+            j.res_vel.assign(4 * j.spec.n, 0.f);
+            int rc = nb_batch_read(s->batch, j.galaxy, j.res_pos.data(), j.res_vel.data());
+            if (rc) return sfail(s, rc, std::string("read result: ") + nb_batch_last_error(s->batch));
+            j.st.state = 2;
+            j.st.done_s = now_s(s);
+            j.galaxy = -1;
+            s->bytes_used -= j.st.bytes;
+            changed = true;
+        } else {
+            keep.push_back(id);
+        }
+    }
+    s->active.swap(keep);
+    if (s->active.empty()) s->dt = NAN;
+    // admit queued jobs (FIFO) while a slot and the budget allow
+    while (!s->queue.empty() && (int)s->active.size() < s->prm.max_active) {
+        Job& j = s->jobs[s->queue.front()];
+        if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
+        if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
+        int rc = generate(j);
+        if (rc) return sfail(s, rc, "job generation failed");
+        j.st.state = 1;
+        j.st.admit_s = now_s(s);
+        j.galaxy = -1;
+        s->bytes_used += j.st.bytes;
+        s->dt = j.spec.dt;
+        s->active.push_back(j.st.id);
+        s->queue.pop_front();
+        changed = true;
+    }
+    if (changed && !s->active.empty()) {
+        int rc = rebuild(s);
+        if (rc) return rc;
+    } else if (s->active.empty() && s->batch) {
+        nb_batch_destroy(s->batch);
+        s->batch = nullptr;
+    }
+    // one round
+    if (!s->active.empty()) {
+        int k = s->prm.steps_per_round;
+        for (uint64_t id : s->active) k = std::min(k, s->jobs[id].spec.steps - s->jobs[id].st.steps_done);
+        k = std::max(k, 1);
+        int rc = nb_batch_step(s->batch, s->dt, k);
+        if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
+        for (uint64_t id : s->active) {
+            Job& j = s->jobs[id];
+            j.st.steps_done += k;
+            s->body_steps += (uint64_t)k * j.spec.n;
+        }
+        ++s->rounds;
+    }
+    if (active) *active = (int)s->active.size();
+    if (queued) *queued = (int)s->queue.size();
+    return NB_OK;
+}
+
+int nb_server_status(nb_server* s, uint64_t id, nb_job_status* out) {
+    if (!s || !out) return NB_EINVAL;
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
+    *out = it->second.st;
+    return NB_OK;
+}
+
+int nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, size_t n) {
+    if (!s) return NB_EINVAL;
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
+    const Job& j = it->second;
+    if (j.st.state != 2) return sfail(s, NB_EBADSTATE, "job not done");
+    if (n != j.spec.n) return sfail(s, NB_EINVAL, "size differs from the job's n");
+    if (pos_mass4) std::memcpy(pos_mass4, j.res_pos.data(), 16 * n);
+    if (vel4) std::memcpy(vel4, j.res_vel.data(), 16 * n);
+    return NB_OK;
+}
+
+int nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds) {
+    if (!s) return NB_EINVAL;
+    if (body_steps) *body_steps = s->body_steps;
+    if (rounds) *rounds = s->rounds;
+    return NB_OK;
+}
+
+}  // extern "C"
