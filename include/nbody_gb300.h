@@ -367,6 +367,21 @@ int  nb_seed_disk(uint64_t seed, size_t n, double total_mass, double rd, double 
  * centre-of-mass frame. */
 int  nb_seed_collision(uint64_t seed, size_t n, double a, double separation,
                        double pericentre, float* pos_mass4, float* vel4);
+/* The reference's own seeders (src/Sim/IParticleSeeder.hpp:12-50), filling
+ * reference records: 0 Random (src/Sim/RandomSeeder.cpp:12-40), 1 Galaxy
+ * (src/Sim/GalaxySeeder.cpp:43-144), 2 StarSystem
+ * (src/Sim/StarSystemSeeder.cpp:17-55), in the reference's units.  The
+ * distributions follow the reference; the random streams cannot
+ * (std::default_random_engine is implementation-defined). */
+int  nb_seed_reference(int seeder, uint64_t seed, float scale, nb_particle* out, size_t n);
+
+/* ---- .nbody files (src/States/Simulation/SimulationState.cpp:229-332) ---- */
+/* Raw little-endian nb_particle records.  nb_file_read stores the record
+ * count in *n (pass particles = NULL to query it) and, like
+ * InitParticlesFromFile, re-centres the positions on the centre of mass when
+ * recentre != 0. */
+int  nb_file_write(const char* path, const nb_particle* particles, size_t n);
+int  nb_file_read(const char* path, nb_particle* particles, size_t capacity, size_t* n, int recentre);
 #ifdef __cplusplus
 }
 #endif

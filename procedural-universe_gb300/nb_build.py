@@ -67,6 +67,27 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int | None = N
     return LIB
 
 
+DRIVER_SRC = os.path.join(HERE, "driver", "nbody_driver.cpp")
+DRIVER = os.path.join(HERE, "nbody_driver")
+
+
+def build_driver(force: bool = False) -> str:
+    """Builds the headless precompute driver against libnbody_gb300.so."""
+    build()
+    deps = [DRIVER_SRC, LIB, os.path.join(INCLUDE, "cuda_nbody_sim.hpp"), os.path.join(INCLUDE, "nbody_gb300.h")]
+    if not force and os.path.exists(DRIVER) and all(os.path.getmtime(d) <= os.path.getmtime(DRIVER) for d in deps):
+        return DRIVER
+    tmp = DRIVER + ".tmp.%d" % os.getpid()
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", INCLUDE, DRIVER_SRC, "-o", tmp,
+           "-L", HERE, "-lnbody_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv)
     print(LIB)
+    print(build_driver(force="--force" in sys.argv))

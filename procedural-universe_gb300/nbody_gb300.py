@@ -139,6 +139,9 @@ def lib() -> ctypes.CDLL:
             "nb_seed_plummer": ([ctypes.c_uint64, sz, f64, f64, vp, vp], i32),
             "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
             "nb_seed_collision": ([ctypes.c_uint64, sz, f64, f64, f64, vp, vp], i32),
+            "nb_seed_reference": ([i32, ctypes.c_uint64, f32, vp, sz], i32),
+            "nb_file_write": ([ctypes.c_char_p, vp, sz], i32),
+            "nb_file_read": ([ctypes.c_char_p, vp, sz, vp, i32], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -189,6 +192,41 @@ def seed_collision(seed: int, n: int, a=1.0, separation=10.0, pericentre=1.0):
     if rc:
         raise NBodyError(rc, "nb_seed_collision")
     return pm, v
+
+
+SEEDER_RANDOM, SEEDER_GALAXY, SEEDER_STAR_SYSTEM = 0, 1, 2
+
+
+def seed_reference(seeder: int, seed: int, n: int, scale: float = 1.0) -> np.ndarray:
+    """Particle records drawn from the reference's RandomSeeder / GalaxySeeder /
+    StarSystemSeeder distributions (src/Sim/*Seeder.cpp)."""
+    p = np.zeros(n, dtype=PARTICLE_DTYPE)
+    rc = lib().nb_seed_reference(seeder, seed, scale, _ptr(p), n)
+    if rc:
+        raise NBodyError(rc, "nb_seed_reference")
+    return p
+
+
+def file_write(path: str, particles: np.ndarray) -> None:
+    """Writes raw 104-byte Particle records (the reference's .nbody file)."""
+    p = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+    rc = lib().nb_file_write(os.fsencode(path), _ptr(p), p.shape[0])
+    if rc:
+        raise NBodyError(rc, "nb_file_write(%s)" % path)
+
+
+def file_read(path: str, recentre: bool = True) -> np.ndarray:
+    """Reads a .nbody file; recentre=True shifts positions to the centre of
+    mass as the reference's file loader does."""
+    n = ctypes.c_size_t(0)
+    rc = lib().nb_file_read(os.fsencode(path), None, 0, ctypes.byref(n), 0)
+    if rc:
+        raise NBodyError(rc, "nb_file_read(%s)" % path)
+    p = np.zeros(n.value, dtype=PARTICLE_DTYPE)
+    rc = lib().nb_file_read(os.fsencode(path), _ptr(p), n.value, ctypes.byref(n), int(recentre))
+    if rc:
+        raise NBodyError(rc, "nb_file_read(%s)" % path)
+    return p[: n.value]
 
 
 def records_from_soa(pos_mass: np.ndarray, vel: np.ndarray | None = None) -> np.ndarray:
