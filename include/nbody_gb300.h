@@ -266,6 +266,9 @@ int  nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4);
 /* Forces (n x 3 doubles) of one galaxy at the current state. */
 int  nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3);
 int  nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last);
+/* Forest of the last step: stats4 = {traversal groups, internal nodes, cells,
+ * Barnes-Hut bodies}. */
+int  nb_batch_tree_stats(nb_batch* b, int64_t* stats4);
 /* Whole-batch state transfer, galaxies in index order concatenated (the sum
  * of their n bodies x float4): upload from / download to host buffers. */
 int  nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4);

@@ -41,8 +41,10 @@ struct nb_batch {
     float4* gal_box = nullptr;
     int32_t* gal_root = nullptr;
     int32_t* slot_start = nullptr;
-    int4* warps = nullptr;
-    int nwarps = 0;
+    int4* groups = nullptr;          // traversal groups, rebuilt on the device every step
+    int group_cap = 0;
+    int* group_ctr = nullptr;        // [0] groups emitted, [1] next group to traverse
+    unsigned* box_bits = nullptr;    // 6 ordered words per galaxy: min xyz, max xyz
     float4* cell_q1 = nullptr;
     float4* cell_q2 = nullptr;
     int32_t* cell_first = nullptr;
@@ -162,7 +164,10 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
         const size_t nk = pad_up((size_t)n, (size_t)tree_sort_tile());
         {
             PhaseScope ps(c, NB_PHASE_KEYS, 2);
-            k_gal_box<<<b->nslot, 256, 0, st>>>(c->pos, b->gal_range, b->nslot, b->gal_box);
+            k_gal_box_init<<<(6 * b->nslot + 255) / 256, 256, 0, st>>>(b->box_bits, b->nslot);
+            k_gal_box_chunks<<<(unsigned)((n + kBoxChunk - 1) / kBoxChunk), 256, 0, st>>>(c->pos, b->body_slot, n,
+                                                                                       b->nslot, b->box_bits);
+            k_gal_box_final<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->box_bits, b->nslot, b->gal_box);
             k_batch_keys<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(c->pos, b->body_slot, n, (int)nk, b->gal_box,
                                                                       t.keys[0], t.vals[0], t.depth);
         }
@@ -178,17 +183,27 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
                                                                  t.int_cell, t.counters + TC_NINT, (int)t.int_cap,
                                                                  b->gal_root,
                                                                  c->d_err);
+            NB_BCUDA(b, cudaMemsetAsync(b->group_ctr, 0, 2 * sizeof(int), st));
+            k_batch_groups<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
+                (int)t.int_cap, t.counters + TC_NINT, t.int_cell, t.cell_meta, t.cell_count, b->cell_first, t.cell_hi,
+                t.vals[0], b->body_slot, (int)t.cell_cap, n, b->groups, b->group_cap, b->group_ctr, c->d_err);
         }
         {
             PhaseScope ps(c, NB_PHASE_TRAVERSE);
             const float th = (float)b->bh_theta;
-            const int blocks = (b->nwarps + kGWarps - 1) / kGWarps;
+            // persistent: as many warps as fit on the GPU, groups taken from the queue
+            int occ = 1;
+            if (b->base.law == NB_LAW_PLUMMER)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_group_traverse<NB_LAW_PLUMMER>, kGWarps * 32, 0);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_group_traverse<NB_LAW_REFERENCE>, kGWarps * 32, 0);
+            const int max_blocks = (b->group_cap + kGWarps - 1) / kGWarps;
+            const int blocks = std::max(1, std::min(max_blocks, c->sm_count * std::max(1, occ)));
 #define NB_GT(L)                                                                                                  \
-    k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(b->warps, b->nwarps, t.spos, t.vals[0], t.cell_com,      \
-                                                        t.cell_meta, b->cell_q1, b->cell_q2, b->cell_first,      \
-                                                        t.cell_count, t.cell_hi, b->gal_box, b->gal_root,        \
-                                                        (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size,   \
-                                                        th * th, S, G, c->acc, t.interactions, c->d_err)
+    k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(                                                         \
+        b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, t.cell_meta,      \
+        b->cell_q1, b->cell_q2, b->cell_first, t.cell_count, t.cell_hi, b->gal_box, b->gal_root, b->nslot,        \
+        (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
             else NB_GT(NB_LAW_REFERENCE);
 #undef NB_GT
@@ -383,8 +398,9 @@ int nb_batch_destroy(nb_batch* b) {
     if (b->core) cudaSetDevice(b->core->dev);
     if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->warps, b->cell_q1,
-                    b->cell_q2, b->cell_first, b->body_dgal, b->dgal, b->units, b->unit_comp, b->part, b->next_unit};
+    void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
+                    b->box_bits, b->cell_q1, b->cell_q2, b->cell_first, b->body_dgal, b->dgal, b->units,
+                    b->unit_comp, b->part, b->next_unit};
     for (void* p : ptrs) cudaFree(p);
     if (b->core) nb_destroy(b->core);
     delete b;
@@ -444,7 +460,7 @@ int nb_batch_commit(nb_batch* b) {
     if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
     std::vector<float> pos(4 * b->n_total, 0.f), vel(4 * b->n_total, 0.f);
     std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
-    std::vector<int4> gal_range(b->nslot), warps;
+    std::vector<int4> gal_range(b->nslot);
     b->n_real = 0;
     for (size_t k = 0; k < b->gal.size(); ++k) {
         const auto& g = b->gal[k];
@@ -457,8 +473,6 @@ int nb_batch_commit(nb_batch* b) {
             for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
             slot_start[g.idx] = (int)g.off;
             gal_range[g.idx] = make_int4((int)g.off, (int)g.n, 0, 0);
-            for (size_t w = 0; w < g.n; w += 32)
-                warps.push_back(make_int4(g.idx, (int)(g.off + w), (int)std::min<size_t>(32, g.n - w), 0));
         } else {
             for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
         }
@@ -476,12 +490,15 @@ int nb_batch_commit(nb_batch* b) {
     NB_BCUDA(b, upload(&b->body_slot, body_slot));
     NB_BCUDA(b, upload(&b->slot_start, slot_start));
     NB_BCUDA(b, upload(&b->gal_range, gal_range));
-    NB_BCUDA(b, upload(&b->warps, warps));
     NB_BCUDA(b, upload(&b->body_dgal, body_dgal));
-    b->nwarps = (int)warps.size();
     if (b->nslot > 0) {
         NB_BCUDA(b, cudaMalloc(&b->gal_box, b->nslot * sizeof(float4)));
         NB_BCUDA(b, cudaMalloc(&b->gal_root, b->nslot * sizeof(int32_t)));
+        NB_BCUDA(b, cudaMalloc(&b->box_bits, 6 * b->nslot * sizeof(unsigned)));
+        // groups are disjoint and non-empty: at most one per body
+        b->group_cap = (int)b->n_bh;
+        NB_BCUDA(b, cudaMalloc(&b->groups, b->n_bh * sizeof(int4)));
+        NB_BCUDA(b, cudaMalloc(&b->group_ctr, 2 * sizeof(int)));
     }
     b->h_pos.clear();
     b->h_vel.clear();
@@ -581,6 +598,23 @@ int nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* inter
         }
         *interactions_last = (uint64_t)v + b->direct_pairs;
     }
+    return NB_OK;
+}
+
+int nb_batch_tree_stats(nb_batch* b, int64_t* stats4) {
+    if (!b || !stats4) return NB_EINVAL;
+    for (int k = 0; k < 4; ++k) stats4[k] = 0;
+    if (!b->committed || b->n_bh == 0) return NB_OK;
+    cudaSetDevice(b->core->dev);
+    int32_t h[TC_COUNT];
+    int rc = read_tree_counts(b, h);
+    if (rc) return rc;
+    int ctr[2] = {0, 0};
+    NB_BCUDA(b, cudaMemcpy(ctr, b->group_ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
+    stats4[0] = ctr[0];
+    stats4[1] = h[TC_NINT];
+    stats4[2] = (int64_t)h[TC_NINT] + h[TC_NLEAF];
+    stats4[3] = (int64_t)b->n_bh;
     return NB_OK;
 }
 

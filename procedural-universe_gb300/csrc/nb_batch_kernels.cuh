@@ -7,15 +7,18 @@
 //    levels), so ONE radix sort and ONE topology build make a forest whose
 //    level-7 nodes are the galaxy roots.
 //  * The mass pass adds traceless quadrupole moments (parallel-axis rule
-//    bottom-up), and the traversal is group-wise: a warp takes up to 32
-//    consecutive sorted bodies of one galaxy, opens a cell when the cell
-//    side exceeds theta times the distance from the cell's centre of mass to
-//    the group's bounding box, and collects accepted cells (monopole +
-//    quadrupole) and leaf buckets of at most leaf_size bodies (summed body by
-//    body) in shared-memory lists that every lane then evaluates -- no lane
-//    idles on a per-lane decision.  This is a performance form whose parity
-//    is the force error against the FP64 direct sum (<= 1e-3), not the
-//    reference's per-body opening rule.
+//    bottom-up).  Traversal groups are taken from the tree itself: the
+//    largest subtrees of at most kGroupMax bodies, consecutive small siblings
+//    packed together, oversized depth-cap buckets cut into chunks -- so a
+//    group is spatially compact and its bounding box small.  A warp takes
+//    groups from a device queue (two bodies per lane), opens a cell when the
+//    cell side exceeds theta times the distance from the cell's centre of
+//    mass to the group's bounding box, and collects accepted cells (monopole
+//    + quadrupole) and leaf buckets of at most leaf_size bodies (summed body
+//    by body) in shared-memory lists that every lane then evaluates for both
+//    of its bodies with the packed FP32x2 instructions.  This is a
+//    performance form whose parity is the force error against the FP64
+//    direct sum (<= 1e-3), not the reference's per-body opening rule.
 //  * Direct-sum members are padded to multiples of 256 bodies; a persistent
 //    kernel takes (galaxy, target block, source range) units from a table
 //    through an atomic counter, and a second kernel folds the partials.
@@ -27,43 +30,86 @@ constexpr int kSlotLevels = 7;          // 21 bits of galaxy slot
 constexpr int kMortonLevels = 14;       // 42 bits of position in the galaxy cube
 constexpr int kBatchDepth = kSlotLevels + kMortonLevels;
 constexpr int kGWarps = 4;              // warps per traversal block
-constexpr int kGStack = 128;            // cells waiting to be opened, per warp
+constexpr int kGroupMax = 64;           // bodies per traversal group (two per lane)
+constexpr int kBoxChunk = 8192;         // bodies per block of the bounding-box pass
+constexpr int kGStack = 512;            // cells waiting to be opened, per warp (<= 32 pushed per step)
 constexpr int kGCells = 64;             // accepted-cell list, per warp
-constexpr int kGRanges = 32;            // leaf-bucket list, per warp
+constexpr int kGBodies = 192;           // gathered leaf-bucket bodies, per warp
 constexpr int kDirTile = 128;           // sources per shared tile of the batched direct kernel
 
 enum : int { BK_SINGLE = 1, BK_BUCKET = 2, BK_INTERNAL = 3 };
 
-// ---- bounding cube of each Barnes-Hut galaxy (one block per galaxy) -------
-__global__ void k_gal_box(const float4* __restrict__ pos, const int4* __restrict__ gal /* off, n */, int ngal,
-                          float4* __restrict__ box) {
-    const int g = blockIdx.x;
-    if (g >= ngal) return;
-    const int4 gi = gal[g];
+// ---- bounding cube of each Barnes-Hut galaxy ------------------------------
+// Min/max are exact and order-free, so chunks of kBoxChunk bodies reduce in
+// parallel into per-galaxy words with atomics on an order-preserving integer
+// image of the float (total order: -inf < ... < -0 < +0 < ... < +inf).
+__device__ __forceinline__ unsigned float_to_ordered(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(unsigned o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+__global__ void k_gal_box_init(unsigned* __restrict__ bits, int nslot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nslot) bits[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
+}
+
+__device__ __forceinline__ void box_flush(unsigned* bits, int slot, const float lo[3], const float hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        atomicMin(&bits[6 * slot + a], float_to_ordered(lo[a]));
+        atomicMax(&bits[6 * slot + 3 + a], float_to_ordered(hi[a]));
+    }
+}
+
+// block b reduces bodies [b*kBoxChunk, (b+1)*kBoxChunk) of the Barnes-Hut range
+__global__ void __launch_bounds__(256) k_gal_box_chunks(const float4* __restrict__ pos,
+                                                        const int32_t* __restrict__ body_slot, int n, int nslot,
+                                                        unsigned* __restrict__ bits) {
+    const int base = blockIdx.x * kBoxChunk;
+    const int end = min(n, base + kBoxChunk);
+    int cur = -1;
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = threadIdx.x; i < gi.y; i += blockDim.x) {
-        const float4 p = pos[gi.x + i];
+    for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
+        const int s = body_slot[i];
+        if (s < 0 || s >= nslot) continue;
+        if (s != cur) {
+            if (cur >= 0) box_flush(bits, cur, lo, hi);
+            cur = s;
+            lo[0] = lo[1] = lo[2] = INFINITY;
+            hi[0] = hi[1] = hi[2] = -INFINITY;
+        }
+        const float4 p = pos[i];
         lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
         hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
     }
-    __shared__ float sh[6][32];
+    // common case: the whole warp ended in one galaxy -> one set of atomics per warp
+    const int lane = threadIdx.x & 31;
+    const int c0 = __shfl_sync(0xffffffffu, cur, 0);
+    if (__all_sync(0xffffffffu, cur == c0)) {
+        for (int a = 0; a < 3; ++a)
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+                hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+            }
+        if (lane == 0 && c0 >= 0) box_flush(bits, c0, lo, hi);
+    } else if (cur >= 0) {
+        box_flush(bits, cur, lo, hi);
+    }
+}
+
+__global__ void k_gal_box_final(const unsigned* __restrict__ bits, int nslot, float4* __restrict__ box) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nslot) return;
+    float lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
-        }
+        lo[a] = ordered_to_float(bits[6 * g + a]);
+        hi[a] = ordered_to_float(bits[6 * g + 3 + a]);
     }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0)
-        for (int a = 0; a < 3; ++a) { sh[a][w] = lo[a]; sh[3 + a][w] = hi[a]; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < nw; ++k)
-            for (int a = 0; a < 3; ++a) { lo[a] = fminf(lo[a], sh[a][k]); hi[a] = fmaxf(hi[a], sh[3 + a][k]); }
-        float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-        ext = fmaxf(ext * 1.001f, 1e-20f);
-        box[g] = make_float4(lo[0], lo[1], lo[2], ext);
-    }
+    float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    ext = fmaxf(ext * 1.001f, 1e-20f);
+    box[g] = make_float4(lo[0], lo[1], lo[2], ext);
 }
 
 __device__ __forceinline__ uint64_t spread3(uint32_t v) {   // 14 bits -> every third bit
@@ -272,68 +318,243 @@ __device__ __forceinline__ void cell_accel(const float4 p, const float4 cm, cons
     az += fmaf(w + c, dz, -qz * ir5);
 }
 
+// ---- traversal groups from the tree --------------------------------------------
+// One thread per internal node at or below the galaxy roots.  A node with more
+// than kGroupMax bodies packs its consecutive children of at most kGroupMax
+// bodies into groups (children are contiguous in sorted order) and cuts a
+// larger depth-cap bucket into chunks; a galaxy root of at most kGroupMax
+// bodies is one group.  Every body lands in exactly one group.
+__device__ __forceinline__ void emit_group(int first, int count, const int32_t* sorder, const int32_t* body_slot,
+                                           int nbodies, int4* groups, int cap, int* n_groups, int* err) {
+    if (count <= 0) return;
+    if (first < 0 || first + count > nbodies) {
+        record_error(err, DEV_TREE_OVERFLOW);
+        return;
+    }
+    const int idx = atomicAdd(n_groups, 1);
+    if (idx >= cap) {
+        record_error(err, DEV_TREE_OVERFLOW);
+        return;
+    }
+    groups[idx] = make_int4(body_slot[sorder[first]], first, count, 0);
+}
+
+__global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_dev, const int32_t* __restrict__ int_cell,
+                               const int4* __restrict__ cell_meta, const int32_t* __restrict__ cell_count,
+                               const int32_t* __restrict__ cell_first, const float4* __restrict__ cell_hi,
+                               const int32_t* __restrict__ sorder, const int32_t* __restrict__ body_slot, int n_cells,
+                               int nbodies, int4* __restrict__ groups, int cap, int* __restrict__ n_groups,
+                               int* __restrict__ err) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= min(*n_int_dev, int_cap)) return;
+    const int c = int_cell[k];
+    if (c < 0 || c >= n_cells) {
+        record_error(err, DEV_TREE_OVERFLOW);
+        return;
+    }
+    const int level = (int)cell_hi[c].w;
+    const int cnt = cell_count[c];
+    if (level < kSlotLevels) return;
+    if (cnt <= kGroupMax) {
+        if (level == kSlotLevels) emit_group(cell_first[c], cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
+        return;   // otherwise an ancestor groups it
+    }
+    const int4 pm = cell_meta[c];
+    const int F = pm.x, nch = (pm.w >> 4) & 15;
+    if (F < 1 || nch > 8 || F + nch > n_cells) {
+        record_error(err, DEV_TREE_OVERFLOW);
+        return;
+    }
+    int run_first = -1, run_cnt = 0;
+    for (int j = 0; j < nch; ++j) {
+        const int ch = F + j;
+        const int4 mt = cell_meta[ch];
+        const int kind = mt.w & 15;
+        const int cc = cell_count[ch];
+        const int cf = kind == BK_INTERNAL ? cell_first[ch] : mt.x;
+        if (cc > kGroupMax) {
+            emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
+            run_first = -1;
+            run_cnt = 0;
+            if (kind != BK_INTERNAL)   // an oversized depth-cap bucket
+                for (int o = 0; o < cc; o += kGroupMax)
+                    emit_group(cf + o, min(kGroupMax, cc - o), sorder, body_slot, nbodies, groups, cap, n_groups, err);
+            continue;                  // an internal child groups its own children
+        }
+        if (run_cnt + cc > kGroupMax) {
+            emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
+            run_first = -1;
+            run_cnt = 0;
+        }
+        if (run_first < 0) run_first = cf;
+        run_cnt += cc;
+    }
+    emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
+}
+
+// The two interactions of a lane (bodies p0 and p1, negated coordinates in
+// n*) with one accepted cell: monopole with the force law plus the Newtonian
+// quadrupole term, in packed FP32x2 arithmetic.
+template <int LAW>
+__device__ __forceinline__ void cell_accel_x2(const float4 cm, const float4 q1, const float4 q2, float2 nx, float2 ny,
+                                              float2 nz, float2 S2, float2& ax, float2& ay, float2& az) {
+    const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+    const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+    const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+    float2 r2 = __fmul2_rn(dx, dx);
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dz, dz, r2);
+    const float2 m2 = make_float2(cm.w, cm.w);
+    float2 w;
+    if (LAW == NB_LAW_REFERENCE) {
+        const float2 s = __fadd2_rn(r2, S2);
+        const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, make_float2(kTiny, kTiny));
+        w = __fmul2_rn(m2, make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y)));
+    } else {
+        const float2 q = __fadd2_rn(r2, S2);
+        const float2 inv = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+        w = __fmul2_rn(__fmul2_rn(m2, inv), __fmul2_rn(inv, inv));
+    }
+    const float2 ir = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+    const float2 ir2 = __fmul2_rn(ir, ir);
+    const float2 ir5 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir);
+    const float2 qx = __ffma2_rn(make_float2(q1.x, q1.x), dx,
+                                 __ffma2_rn(make_float2(q2.x, q2.x), dy, __fmul2_rn(make_float2(q2.y, q2.y), dz)));
+    const float2 qy = __ffma2_rn(make_float2(q2.x, q2.x), dx,
+                                 __ffma2_rn(make_float2(q1.y, q1.y), dy, __fmul2_rn(make_float2(q2.z, q2.z), dz)));
+    const float2 qz = __ffma2_rn(make_float2(q2.y, q2.y), dx,
+                                 __ffma2_rn(make_float2(q2.z, q2.z), dy, __fmul2_rn(make_float2(q1.z, q1.z), dz)));
+    const float2 xqx = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+    const float2 c = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(2.5f, 2.5f), xqx), ir5), ir2);
+    const float2 wc = __fadd2_rn(w, c);
+    const float2 nir5 = make_float2(-ir5.x, -ir5.y);
+    ax = __fadd2_rn(ax, __ffma2_rn(wc, dx, __fmul2_rn(qx, nir5)));
+    ay = __fadd2_rn(ay, __ffma2_rn(wc, dy, __fmul2_rn(qy, nir5)));
+    az = __fadd2_rn(az, __ffma2_rn(wc, dz, __fmul2_rn(qz, nir5)));
+}
+
+__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2& t) {
+    kahan_add(s.x, c.x, t.x);
+    kahan_add(s.y, c.y, t.y);
+    t = make_float2(0.f, 0.f);
+}
+
+// Persistent: each warp takes groups from the queue until it is empty.
 template <int LAW>
 __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
-    const int4* __restrict__ warps, int nwarps, const float4* __restrict__ spos, const int32_t* __restrict__ sorder,
-    const float4* __restrict__ cell_com, const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1,
-    const float4* __restrict__ cell_q2, const int32_t* __restrict__ cell_first, const int32_t* __restrict__ cell_count,
-    const float4* __restrict__ cell_hi, const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root,
-    int n_cells, int nbodies, int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
+    const int4* __restrict__ groups, const int* __restrict__ n_groups_dev, int group_cap, int* __restrict__ next_group,
+    const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const float4* __restrict__ cell_com,
+    const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
+    const int32_t* __restrict__ cell_first, const int32_t* __restrict__ cell_count, const float4* __restrict__ cell_hi,
+    const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
+    int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
     __shared__ float4 lcm[kGWarps][kGCells], lq1[kGWarps][kGCells], lq2[kGWarps][kGCells];
-    __shared__ int2 lrg[kGWarps][kGRanges];
-    __shared__ float4 bbuf[kGWarps][32];
+    __shared__ float4 lbd[kGWarps][kGBodies];
+    __shared__ int rinc[kGWarps][32], rfst[kGWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kGWarps + w;
-    if (gw >= nwarps) return;   // whole warp
-    const int4 wi = warps[gw];  // (slot, first sorted position, count, 0)
-    const bool valid = lane < wi.z;
-    const int s = wi.y + (valid ? lane : 0);
-    const float4 p = spos[s];
-    float bl[3] = {valid ? p.x : INFINITY, valid ? p.y : INFINITY, valid ? p.z : INFINITY};
-    float bh[3] = {valid ? p.x : -INFINITY, valid ? p.y : -INFINITY, valid ? p.z : -INFINITY};
-    for (int a = 0; a < 3; ++a)
-        for (int o = 16; o > 0; o >>= 1) {
-            bl[a] = fminf(bl[a], __shfl_xor_sync(0xffffffffu, bl[a], o));
-            bh[a] = fmaxf(bh[a], __shfl_xor_sync(0xffffffffu, bh[a], o));
-        }
-    const float4 gb = gal_box[wi.x];
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
-    unsigned cnt = 0;
-    int nst = 0, ncl = 0, nrg = 0, pops = 0;
-    bool bad = false;
     const uint32_t lt = (1u << lane) - 1u;
+    const int ngroups = min(*n_groups_dev, group_cap);
+    const float2 S2 = make_float2(S, S);
+    unsigned long long total = 0;
+    for (;;) {
+    int gi = 0;
+    if (lane == 0) gi = atomicAdd(next_group, 1);
+    gi = __shfl_sync(0xffffffffu, gi, 0);
+    if (gi >= ngroups) break;
+    const int4 grp = groups[gi];   // (slot, first sorted position, count, 0)
+    if (grp.x < 0 || grp.x >= nslot || grp.y < 0 || grp.z < 1 || grp.z > kGroupMax || grp.y + grp.z > nbodies) {
+        if (lane == 0) record_error(err, DEV_TREE_OVERFLOW);
+        continue;
+    }
+    const bool v0 = lane < grp.z, v1 = lane + 32 < grp.z;
+    const int s0 = grp.y + (v0 ? lane : 0), s1 = grp.y + (v1 ? lane + 32 : 0);
+    const float4 p0 = spos[s0], p1 = spos[s1];
+    float bl[3], bh[3];
+    {
+        const float a0[3] = {p0.x, p0.y, p0.z}, a1[3] = {p1.x, p1.y, p1.z};
+        for (int a = 0; a < 3; ++a) {
+            bl[a] = fminf(v0 ? a0[a] : INFINITY, v1 ? a1[a] : INFINITY);
+            bh[a] = fmaxf(v0 ? a0[a] : -INFINITY, v1 ? a1[a] : -INFINITY);
+            for (int o = 16; o > 0; o >>= 1) {
+                bl[a] = fminf(bl[a], __shfl_xor_sync(0xffffffffu, bl[a], o));
+                bh[a] = fmaxf(bh[a], __shfl_xor_sync(0xffffffffu, bh[a], o));
+            }
+        }
+    }
+    const float2 nx = make_float2(-p0.x, -p1.x), ny = make_float2(-p0.y, -p1.y), nz = make_float2(-p0.z, -p1.z);
+    const float4 gb = gal_box[grp.x];
+    float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx, cx = sx, cy = sx, cz = sx, tx = sx, ty = sx, tz = sx;
+    unsigned cnt = 0;
+    const unsigned nv = (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
+    int nst = 0, ncl = 0, nbd = 0, pops = 0;
+    bool bad = false;
 
     auto flush_cells = [&]() {
         __syncwarp();
-        for (int i = 0; i < ncl; ++i) cell_accel<LAW>(p, lcm[w][i], lq1[w][i], lq2[w][i], S, tx, ty, tz);
-        cnt += valid ? ncl : 0;
+        for (int i = 0; i < ncl; ++i) cell_accel_x2<LAW>(lcm[w][i], lq1[w][i], lq2[w][i], nx, ny, nz, S2, tx, ty, tz);
+        cnt += nv * ncl;
         ncl = 0;
-        kahan_add(sx, cx, tx); kahan_add(sy, cy, ty); kahan_add(sz, cz, tz);
-        tx = ty = tz = 0.f;
+        kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
         __syncwarp();
     };
-    auto flush_ranges = [&]() {
+    auto flush_bodies = [&]() {
         __syncwarp();
-        for (int r = 0; r < nrg; ++r) {
-            const int2 rg = lrg[w][r];
-            for (int b0 = 0; b0 < rg.y; b0 += 32) {
-                const int m = min(32, rg.y - b0);
-                if (lane < m) bbuf[w][lane] = spos[rg.x + b0 + lane];
-                __syncwarp();
-                for (int j = 0; j < m; ++j) body_accel<LAW>(p, bbuf[w][j], S, tx, ty, tz);
-                cnt += valid ? m : 0;
-                __syncwarp();
+        int j = 0;
+#pragma unroll 1
+        for (; j + 4 <= nbd; j += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float4 b = lbd[w][j + u];
+                interact_x2<LAW>(make_float2(b.x, b.x), make_float2(b.y, b.y), make_float2(b.z, b.z),
+                                 make_float2(b.w, b.w), nx, ny, nz, S2, tx, ty, tz);
             }
-            kahan_add(sx, cx, tx); kahan_add(sy, cy, ty); kahan_add(sz, cz, tz);
-            tx = ty = tz = 0.f;
         }
-        nrg = 0;
+        for (; j < nbd; ++j) {
+            const float4 b = lbd[w][j];
+            interact_x2<LAW>(make_float2(b.x, b.x), make_float2(b.y, b.y), make_float2(b.z, b.z),
+                             make_float2(b.w, b.w), nx, ny, nz, S2, tx, ty, tz);
+        }
+        cnt += nv * nbd;
+        nbd = 0;
+        kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
         __syncwarp();
+    };
+    // Appends the bodies of this step's accepted leaf ranges (lane l: first,
+    // count; count 0 for lanes without one) to the body list, all lanes
+    // copying, evaluating the list whenever it fills.
+    auto gather_ranges = [&](int first, int count) {
+        int incl = count;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int tot = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        rinc[w][lane] = incl;
+        rfst[w][lane] = first;
+        __syncwarp();
+        for (int done = 0; done < tot;) {
+            if (nbd == kGBodies) flush_bodies();
+            const int take = min(kGBodies - nbd, tot - done);
+            for (int j = lane; j < take; j += 32) {
+                const int jj = done + j;
+                int lo = 0, hi = 31;   // owner: the first lane whose inclusive end exceeds jj
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (rinc[w][mid] > jj) hi = mid; else lo = mid + 1;
+                }
+                const int base = lo > 0 ? rinc[w][lo - 1] : 0;
+                lbd[w][nbd + j] = spos[rfst[w][lo] + (jj - base)];
+            }
+            nbd += take;
+            done += take;
+            __syncwarp();
+        }
     };
 
-    const int root = gal_root[wi.x];
+    const int root = gal_root[grp.x];
     if (root < 1 || root >= n_cells) {
         bad = true;
     } else {
@@ -343,16 +564,40 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
     __syncwarp();
     while (nst > 0 && !bad) {
         if (++pops > max_pops) { bad = true; break; }
-        const int c = stk[w][--nst];
+        // Take up to 8 opened cells from the top of the stack, as many as have
+        // at most 32 children together; lane j tests the j-th of those children.
+        int pF = 0, pn = 0;
+        bool p_bad = false;
+        if (lane < 8 && lane < nst) {
+            const int c = stk[w][nst - 1 - lane];
+            const int4 pm = __ldg(&cell_meta[c]);
+            pF = pm.x;
+            pn = (pm.w >> 4) & 15;
+            if ((pm.w & 15) != BK_INTERNAL || pF < 1 || pn > 8 || pF + pn > n_cells) p_bad = true, pn = 0;
+        }
+        if (__any_sync(0xffffffffu, p_bad)) { bad = true; break; }
+        int incl = pn;   // inclusive prefix of the child counts over lanes 0..7
+        for (int o = 1; o < 8; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t take = __ballot_sync(0xffffffffu, lane < 8 && lane < nst && incl <= 32);
+        const int P = __popc(take);   // >= 1: one cell has at most 8 children
+        const int T = __shfl_sync(0xffffffffu, incl, P - 1);
         __syncwarp();
-        const int4 pm = __ldg(&cell_meta[c]);
-        const int F = pm.x, nch = (pm.w >> 4) & 15;
-        if ((pm.w & 15) != BK_INTERNAL || F < 1 || nch > 8 || F + nch > n_cells) { bad = true; break; }
+        nst -= P;
+        int q = 0;   // source cell of this lane's child: the number of taken cells whose prefix ends at or before it
+        for (int l = 0; l < 8; ++l) {
+            const int e = __shfl_sync(0xffffffffu, incl, l);
+            q += (l < P && e <= lane) ? 1 : 0;
+        }
+        const int qF = __shfl_sync(0xffffffffu, pF, q & 7);
+        const int qx = __shfl_sync(0xffffffffu, incl - pn, q & 7);
         bool a_cell = false, a_range = false, a_push = false, a_bad = false;
         float4 ccm = make_float4(0.f, 0.f, 0.f, 0.f);
         int first = 0, count = 0, ch = 0;
-        if (lane < nch) {
-            ch = F + lane;
+        if (lane < T) {
+            ch = qF + (lane - qx);
             ccm = __ldg(&cell_com[ch]);
             const int4 mt = __ldg(&cell_meta[ch]);
             const int kind = mt.w & 15;
@@ -386,11 +631,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
             ncl += __popc(bc);
         }
         const uint32_t br = __ballot_sync(0xffffffffu, a_range);
-        if (br) {
-            if (nrg + __popc(br) > kGRanges) flush_ranges();
-            if (a_range) lrg[w][nrg + __popc(br & lt)] = make_int2(first, count);
-            nrg += __popc(br);
-        }
+        if (br) gather_ranges(a_range ? first : 0, a_range ? count : 0);
         const uint32_t bp = __ballot_sync(0xffffffffu, a_push);
         if (bp) {
             if (nst + __popc(bp) > kGStack) { bad = true; break; }
@@ -401,14 +642,16 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
     }
     if (!bad) {
         flush_cells();
-        flush_ranges();
+        flush_bodies();
     }
-    kahan_add(sx, cx, tx); kahan_add(sy, cy, ty); kahan_add(sz, cz, tz);
+    kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
     if (bad && lane == 0) record_error(err, DEV_STACK_OVERFLOW);
-    if (valid) acc[sorder[s]] = make_float4(G * (sx - cx), G * (sy - cy), G * (sz - cz), 0.f);
-    unsigned long long cc2 = cnt;
-    for (int o = 16; o > 0; o >>= 1) cc2 += __shfl_down_sync(0xffffffffu, cc2, o);
-    if (lane == 0 && cc2) atomicAdd(inter, cc2);
+    if (v0) acc[sorder[s0]] = make_float4(G * (sx.x - cx.x), G * (sy.x - cy.x), G * (sz.x - cz.x), 0.f);
+    if (v1) acc[sorder[s1]] = make_float4(G * (sx.y - cx.y), G * (sy.y - cy.y), G * (sz.y - cz.y), 0.f);
+    total += cnt;
+    }
+    for (int o = 16; o > 0; o >>= 1) total += __shfl_down_sync(0xffffffffu, total, o);
+    if (lane == 0 && total) atomicAdd(inter, total);
 }
 
 // ---- batched direct sum --------------------------------------------------------

@@ -406,6 +406,7 @@ def _bind_batch():
         "nb_batch_read": ([vp, i32, vp, vp], i32),
         "nb_batch_forces": ([vp, i32, vp], i32),
         "nb_batch_info": ([vp, vp, vp, vp], i32),
+        "nb_batch_tree_stats": ([vp, vp], i32),
         "nb_batch_stream": ([vp], vp),
         "nb_batch_write_state": ([vp, vp, vp], i32),
         "nb_batch_read_state": ([vp, vp, vp], i32),
@@ -513,3 +514,8 @@ class NBodyBatch:
         self._check(lib().nb_batch_info(self._h, ctypes.byref(ng), ctypes.byref(nb_), ctypes.byref(it)),
                     "nb_batch_info")
         return dict(galaxies=ng.value, bodies=nb_.value, interactions=it.value)
+
+    def tree_stats(self):
+        s = (ctypes.c_int64 * 4)()
+        self._check(lib().nb_batch_tree_stats(self._h, s), "nb_batch_tree_stats")
+        return dict(groups=s[0], internal=s[1], cells=s[2], bh_bodies=s[3])

@@ -74,8 +74,9 @@ def test_cpp_adapter_program(tmp_path):
 #include <cstdio>
 int main() {
     std::vector<nbgb::Particle> v(2048);
-    nb_seed_reference(1, 3, 1.0f, v.data(), v.size());
-    nb_params p; nb_default_params(&p); p.theta = 0.8;
+    nb_seed_reference(2, 3, 1.0f, v.data(), v.size());
+    nb_params p; nb_default_params(&p);
+    p.G = 6.674e-11; p.softening2 = 10.0; p.pos_scale = 2.3e13; p.theta = 0.8;
     nbgb::CudaNBodySim sim(nbgb::ENBodySim::BarnesHut, &p);
     sim.Init(v);
     const float x0 = v[100].position[0];
