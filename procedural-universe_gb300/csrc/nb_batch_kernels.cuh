@@ -392,56 +392,69 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
     emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
 }
 
-// The two interactions of a lane (bodies p0 and p1, negated coordinates in
-// n*) with one accepted cell: monopole with the force law plus the Newtonian
-// quadrupole term, in packed FP32x2 arithmetic.
+// Interactions of one target (negated coordinates duplicated in both halves
+// of n*) with TWO accepted cells at once (their values paired in the float2
+// operands): monopole with the force law plus the Newtonian quadrupole term,
+//   a += w x - Q x / r^5 + 5/2 (x.Q.x) x / r^7,  x = com - p,
+// w the force law's (softened) monopole factor.
 template <int LAW>
-__device__ __forceinline__ void cell_accel_x2(const float4 cm, const float4 q1, const float4 q2, float2 nx, float2 ny,
-                                              float2 nz, float2 S2, float2& ax, float2& ay, float2& az) {
-    const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
-    const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
-    const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+__device__ __forceinline__ void cell_pair_accel(float2 cx, float2 cy, float2 cz, float2 cm, float2 qxx, float2 qyy,
+                                                float2 qzz, float2 qxy, float2 qxz, float2 qyz, float2 nx, float2 ny,
+                                                float2 nz, float2 S2, float2& ax, float2& ay, float2& az) {
+    const float2 dx = __fadd2_rn(cx, nx);
+    const float2 dy = __fadd2_rn(cy, ny);
+    const float2 dz = __fadd2_rn(cz, nz);
     float2 r2 = __fmul2_rn(dx, dx);
     r2 = __ffma2_rn(dy, dy, r2);
     r2 = __ffma2_rn(dz, dz, r2);
-    const float2 m2 = make_float2(cm.w, cm.w);
     float2 w;
     if (LAW == NB_LAW_REFERENCE) {
         const float2 s = __fadd2_rn(r2, S2);
         const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, make_float2(kTiny, kTiny));
-        w = __fmul2_rn(m2, make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y)));
+        w = __fmul2_rn(cm, make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y)));
     } else {
         const float2 q = __fadd2_rn(r2, S2);
         const float2 inv = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
-        w = __fmul2_rn(__fmul2_rn(m2, inv), __fmul2_rn(inv, inv));
+        w = __fmul2_rn(__fmul2_rn(cm, inv), __fmul2_rn(inv, inv));
     }
     const float2 ir = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
     const float2 ir2 = __fmul2_rn(ir, ir);
-    const float2 ir5 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir);
-    const float2 qx = __ffma2_rn(make_float2(q1.x, q1.x), dx,
-                                 __ffma2_rn(make_float2(q2.x, q2.x), dy, __fmul2_rn(make_float2(q2.y, q2.y), dz)));
-    const float2 qy = __ffma2_rn(make_float2(q2.x, q2.x), dx,
-                                 __ffma2_rn(make_float2(q1.y, q1.y), dy, __fmul2_rn(make_float2(q2.z, q2.z), dz)));
-    const float2 qz = __ffma2_rn(make_float2(q2.y, q2.y), dx,
-                                 __ffma2_rn(make_float2(q2.z, q2.z), dy, __fmul2_rn(make_float2(q1.z, q1.z), dz)));
+    const float2 ir5 = __fmul2_rn(__fmul2_rn(ir2, ir), ir2);
+    const float2 qx = __ffma2_rn(qxx, dx, __ffma2_rn(qxy, dy, __fmul2_rn(qxz, dz)));
+    const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
+    const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
     const float2 xqx = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
-    const float2 c = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(2.5f, 2.5f), xqx), ir5), ir2);
-    const float2 wc = __fadd2_rn(w, c);
-    const float2 nir5 = make_float2(-ir5.x, -ir5.y);
-    ax = __fadd2_rn(ax, __ffma2_rn(wc, dx, __fmul2_rn(qx, nir5)));
-    ay = __fadd2_rn(ay, __ffma2_rn(wc, dy, __fmul2_rn(qy, nir5)));
-    az = __fadd2_rn(az, __ffma2_rn(wc, dz, __fmul2_rn(qz, nir5)));
+    const float2 c7 = __fmul2_rn(ir5, __fmul2_rn(ir2, make_float2(2.5f, 2.5f)));
+    const float2 wc = __ffma2_rn(xqx, c7, w);
+    const float2 nir5 = __fmul2_rn(ir5, make_float2(-1.f, -1.f));
+    ax = __ffma2_rn(wc, dx, __ffma2_rn(nir5, qx, ax));
+    ay = __ffma2_rn(wc, dy, __ffma2_rn(nir5, qy, ay));
+    az = __ffma2_rn(wc, dz, __ffma2_rn(nir5, qz, az));
 }
 
-__device__ __forceinline__ void kahan_add2(float2& s, float2& c, float2& t) {
-    kahan_add(s.x, c.x, t.x);
-    kahan_add(s.y, c.y, t.y);
-    t = make_float2(0.f, 0.f);
+// Shared-memory lists hold their entries in pairs, each value of the two
+// entries side by side, so that one 16-byte load yields two FP32x2 operands:
+// a body pair is (x x' y y')(z z' m m'), a cell pair (x x' y y')(z z' m m')
+// (Qxx Qxx' Qyy Qyy')(Qzz Qzz' Qxy Qxy')(Qxz Qxz' Qyz Qyz').
+constexpr float kFarAway = 1e18f;   // position of the zero-mass cell that pads an odd list
+
+__device__ __forceinline__ void put_body(float4 (*lst)[2], int j, float4 b) {
+    float* f = reinterpret_cast<float*>(lst[j >> 1]);
+    const int h = j & 1;
+    f[h] = b.x; f[2 + h] = b.y; f[4 + h] = b.z; f[6 + h] = b.w;
+}
+
+__device__ __forceinline__ void put_cell(float4 (*lst)[5], int j, float4 cm, float4 q1, float4 q2) {
+    float* f = reinterpret_cast<float*>(lst[j >> 1]);
+    const int h = j & 1;
+    f[h] = cm.x; f[2 + h] = cm.y; f[4 + h] = cm.z; f[6 + h] = cm.w;
+    f[8 + h] = q1.x; f[10 + h] = q1.y; f[12 + h] = q1.z; f[14 + h] = q2.x;
+    f[16 + h] = q2.y; f[18 + h] = q2.z;
 }
 
 // Persistent: each warp takes groups from the queue until it is empty.
 template <int LAW>
-__global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
+__global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const int4* __restrict__ groups, const int* __restrict__ n_groups_dev, int group_cap, int* __restrict__ next_group,
     const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const float4* __restrict__ cell_com,
     const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
@@ -450,8 +463,8 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
     int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
-    __shared__ float4 lcm[kGWarps][kGCells], lq1[kGWarps][kGCells], lq2[kGWarps][kGCells];
-    __shared__ float4 lbd[kGWarps][kGBodies];
+    __shared__ float4 lcl[kGWarps][kGCells / 2][5];
+    __shared__ float4 lbd[kGWarps][kGBodies / 2][2];
     __shared__ int rinc[kGWarps][32], rfst[kGWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
@@ -483,42 +496,73 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
             }
         }
     }
-    const float2 nx = make_float2(-p0.x, -p1.x), ny = make_float2(-p0.y, -p1.y), nz = make_float2(-p0.z, -p1.z);
+    // negated target coordinates, duplicated: the pair partner is the other list entry
+    const float2 n0x = make_float2(-p0.x, -p0.x), n0y = make_float2(-p0.y, -p0.y), n0z = make_float2(-p0.z, -p0.z);
+    const float2 n1x = make_float2(-p1.x, -p1.x), n1y = make_float2(-p1.y, -p1.y), n1z = make_float2(-p1.z, -p1.z);
     const float4 gb = gal_box[grp.x];
-    float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx, cx = sx, cy = sx, cz = sx, tx = sx, ty = sx, tz = sx;
+    const float2 z2 = make_float2(0.f, 0.f);
+    float2 a0x = z2, a0y = z2, a0z = z2, a1x = z2, a1y = z2, a1z = z2;   // (even entries, odd entries)
+    float s0x = 0.f, s0y = 0.f, s0z = 0.f, c0x = 0.f, c0y = 0.f, c0z = 0.f;
+    float s1x = 0.f, s1y = 0.f, s1z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
     unsigned cnt = 0;
     const unsigned nv = (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
     int nst = 0, ncl = 0, nbd = 0, pops = 0;
     bool bad = false;
 
+    auto fold = [&]() {
+        kahan_add(s0x, c0x, a0x.x + a0x.y); kahan_add(s0y, c0y, a0y.x + a0y.y); kahan_add(s0z, c0z, a0z.x + a0z.y);
+        kahan_add(s1x, c1x, a1x.x + a1x.y); kahan_add(s1y, c1y, a1y.x + a1y.y); kahan_add(s1z, c1z, a1z.x + a1z.y);
+        a0x = a0y = a0z = a1x = a1y = a1z = z2;
+    };
     auto flush_cells = [&]() {
+        if (ncl & 1) {   // pad with a zero-mass, zero-moment cell far away: adds exactly zero
+            if (lane == 0)
+                put_cell(lcl[w], ncl, make_float4(kFarAway, kFarAway, kFarAway, 0.f), make_float4(0.f, 0.f, 0.f, 0.f),
+                         make_float4(0.f, 0.f, 0.f, 0.f));
+        }
         __syncwarp();
-        for (int i = 0; i < ncl; ++i) cell_accel_x2<LAW>(lcm[w][i], lq1[w][i], lq2[w][i], nx, ny, nz, S2, tx, ty, tz);
+        for (int k = 0; k < (ncl + 1) >> 1; ++k) {
+            const float4 e0 = lcl[w][k][0], e1 = lcl[w][k][1], e2 = lcl[w][k][2], e3 = lcl[w][k][3], e4 = lcl[w][k][4];
+            const float2 cx = make_float2(e0.x, e0.y), cy = make_float2(e0.z, e0.w), cz = make_float2(e1.x, e1.y);
+            const float2 cm = make_float2(e1.z, e1.w), qxx = make_float2(e2.x, e2.y), qyy = make_float2(e2.z, e2.w);
+            const float2 qzz = make_float2(e3.x, e3.y), qxy = make_float2(e3.z, e3.w), qxz = make_float2(e4.x, e4.y);
+            const float2 qyz = make_float2(e4.z, e4.w);
+            cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+            cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+        }
         cnt += nv * ncl;
         ncl = 0;
-        kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
+        fold();
         __syncwarp();
     };
     auto flush_bodies = [&]() {
+        if (nbd & 1) {   // pad with a zero-mass body: adds exactly zero
+            if (lane == 0) put_body(lbd[w], nbd, make_float4(0.f, 0.f, 0.f, 0.f));
+        }
         __syncwarp();
-        int j = 0;
+        const int np = (nbd + 1) >> 1;
+        int k = 0;
 #pragma unroll 1
-        for (; j + 4 <= nbd; j += 4) {
+        for (; k + 2 <= np; k += 2) {
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const float4 b = lbd[w][j + u];
-                interact_x2<LAW>(make_float2(b.x, b.x), make_float2(b.y, b.y), make_float2(b.z, b.z),
-                                 make_float2(b.w, b.w), nx, ny, nz, S2, tx, ty, tz);
+            for (int u = 0; u < 2; ++u) {
+                const float4 e0 = lbd[w][k + u][0], e1 = lbd[w][k + u][1];
+                const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
+                const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
+                interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+                interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
             }
         }
-        for (; j < nbd; ++j) {
-            const float4 b = lbd[w][j];
-            interact_x2<LAW>(make_float2(b.x, b.x), make_float2(b.y, b.y), make_float2(b.z, b.z),
-                             make_float2(b.w, b.w), nx, ny, nz, S2, tx, ty, tz);
+        for (; k < np; ++k) {
+            const float4 e0 = lbd[w][k][0], e1 = lbd[w][k][1];
+            const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
+            const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
+            interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+            interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
         }
         cnt += nv * nbd;
         nbd = 0;
-        kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
+        fold();
         __syncwarp();
     };
     // Appends the bodies of this step's accepted leaf ranges (lane l: first,
@@ -546,7 +590,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
                     if (rinc[w][mid] > jj) hi = mid; else lo = mid + 1;
                 }
                 const int base = lo > 0 ? rinc[w][lo - 1] : 0;
-                lbd[w][nbd + j] = spos[rfst[w][lo] + (jj - base)];
+                put_body(lbd[w], nbd + j, spos[rfst[w][lo] + (jj - base)]);
             }
             nbd += take;
             done += take;
@@ -624,9 +668,7 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
             if (ncl + __popc(bc) > kGCells) flush_cells();
             if (a_cell) {
                 const int idx = ncl + __popc(bc & lt);
-                lcm[w][idx] = ccm;
-                lq1[w][idx] = __ldg(&cell_q1[ch]);
-                lq2[w][idx] = __ldg(&cell_q2[ch]);
+                put_cell(lcl[w], idx, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]));
             }
             ncl += __popc(bc);
         }
@@ -644,10 +686,10 @@ __global__ void __launch_bounds__(kGWarps * 32) k_group_traverse(
         flush_cells();
         flush_bodies();
     }
-    kahan_add2(sx, cx, tx); kahan_add2(sy, cy, ty); kahan_add2(sz, cz, tz);
+    fold();
     if (bad && lane == 0) record_error(err, DEV_STACK_OVERFLOW);
-    if (v0) acc[sorder[s0]] = make_float4(G * (sx.x - cx.x), G * (sy.x - cy.x), G * (sz.x - cz.x), 0.f);
-    if (v1) acc[sorder[s1]] = make_float4(G * (sx.y - cx.y), G * (sy.y - cy.y), G * (sz.y - cz.y), 0.f);
+    if (v0) acc[sorder[s0]] = make_float4(G * (s0x - c0x), G * (s0y - c0y), G * (s0z - c0z), 0.f);
+    if (v1) acc[sorder[s1]] = make_float4(G * (s1x - c1x), G * (s1y - c1y), G * (s1z - c1z), 0.f);
     total += cnt;
     }
     for (int o = 16; o > 0; o >>= 1) total += __shfl_down_sync(0xffffffffu, total, o);
