@@ -38,6 +38,31 @@ def batch_galaxies(nb, seed=2024, count=512, lo=256, hi=65536):
     return gals
 
 
+PLAIN_THETAS = (0.5, 0.4, 0.35, 0.3, 0.28, 0.26, 0.24, 0.22, 0.2, 0.18, 0.16)
+
+
+def force_error(nb, F, pm, v, eps2, samples=1024, seed=3):
+    """Relative L2 error of forces F against the FP64 direct sum on sampled bodies."""
+    n = pm.shape[0]
+    t = np.sort(np.random.default_rng(seed).choice(n, min(n, samples), replace=False)).astype(np.int32)
+    with nb.NBodySim(kind=nb.SIM_BRUTE_FORCE, softening2=eps2) as s:
+        s.init_soa(pm, v)
+        F64 = s.fp64_forces(t)
+    return float(np.linalg.norm(F[t] - F64) / np.linalg.norm(F64))
+
+
+def plain_theta_for(nb, pm, v, eps2, target=1e-3):
+    """Largest theta of the plain path (the reference's per-body opening rule)
+    whose force error on this galaxy is within target."""
+    for th in PLAIN_THETAS:
+        with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps2, theta=th) as s:
+            s.init_soa(pm, v)
+            e = force_error(nb, s.compute_forces(), pm, v, eps2)
+        if e <= target:
+            return th, e
+    return PLAIN_THETAS[-1], e
+
+
 def sequential_plain(nb, gals, eps2, dt, theta, threshold, steps=2):
     """Body-steps/s of stepping every galaxy with its own plain handle, one after another."""
     total_t = 0.0
@@ -108,27 +133,40 @@ def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, the
     stats = server.stats()
     server.close()
     # sequential plain path: one handle per job (reference per-body Barnes-Hut), FIFO
-    service = []
-    for k, n in enumerate(sizes):
-        t0 = time.perf_counter()
-        pm, v = nb.seed_disk(10_000 + k, int(n))
-        t_gen = time.perf_counter() - t0
-        with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps * eps, theta=theta) as s:
-            s.init_soa(pm, v)
-            s.step(dt, 1)
-            s.synchronize()
+    def replay(th):
+        service = []
+        for k, n in enumerate(sizes):
             t0 = time.perf_counter()
-            s.step(dt, 2)
-            s.synchronize()
-            t_step = (time.perf_counter() - t0) / 2
-        service.append(t_gen + steps * t_step)
-    service = np.array(service)
-    done, t = [], 0.0
-    for arr, sv in zip(arrivals, service):
-        t = max(t, arr) + sv
-        done.append(t)
-    seq_lat = np.array(done) - arrivals
-    seq_value = total / (done[-1] - arrivals[0])
+            pm, v = nb.seed_disk(10_000 + k, int(n))
+            t_gen = time.perf_counter() - t0
+            with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps * eps, theta=th) as s:
+                s.init_soa(pm, v)
+                s.step(dt, 1)
+                s.synchronize()
+                t0 = time.perf_counter()
+                s.step(dt, 2)
+                s.synchronize()
+                t_step = (time.perf_counter() - t0) / 2
+            service.append(t_gen + steps * t_step)
+        done, t = [], 0.0
+        for arr, sv in zip(arrivals, service):
+            t = max(t, arr) + sv
+            done.append(t)
+        lat = np.array(done) - arrivals
+        return total / (done[-1] - arrivals[0]), lat
+
+    seq_value, seq_lat = replay(theta)
+    big = int(np.argmax(sizes))
+    pm, v = nb.seed_disk(10_000 + big, int(sizes[big]))
+    with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps * eps, theta=theta) as s:
+        s.init_soa(pm, v)
+        plain_err = force_error(nb, s.compute_forces(), pm, v, eps * eps)
+    with nb.NBodyBatch(bh_threshold=1024, bh_theta=theta, softening2=eps * eps) as b:
+        b.add(pm, v)
+        b.commit()
+        served_err = force_error(nb, b.forces(0), pm, v, eps * eps)
+    th_eq, err_eq = plain_theta_for(nb, pm, v, eps * eps)
+    eq_value, eq_lat = replay(th_eq)
     return {
         "metric": METRIC, "value": total / makespan, "unit": METRIC, "n_gpus": 1, "steps": steps,
         "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -140,12 +178,19 @@ def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, the
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
         "makespan_s": makespan, "rounds": stats["rounds"],
-        "sequential_plain": {"value": seq_value, "unit": METRIC,
+        "force_rel_l2_vs_fp64_largest": served_err,
+        "sequential_plain": {"value": seq_value, "unit": METRIC, "theta": theta,
+                             "force_rel_l2_vs_fp64_largest": plain_err,
                              "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
                                            "p99": float(np.percentile(seq_lat, 99))},
                              "how": "each job generated then stepped by its own plain Barnes-Hut handle, FIFO, "
                                     "the same arrivals; step time measured over 2 steps and scaled to %d" % steps},
         "speedup_vs_sequential_plain": (total / makespan) / seq_value,
+        "sequential_plain_equal_accuracy": {
+            "value": eq_value, "unit": METRIC, "theta": th_eq, "force_rel_l2_vs_fp64_largest": err_eq,
+            "latency_s": {"p50": float(np.percentile(eq_lat, 50)), "p99": float(np.percentile(eq_lat, 99))},
+            "how": "as sequential_plain, at the largest theta whose force error on the largest job is <= 1e-3"},
+        "speedup_vs_sequential_plain_equal_accuracy": (total / makespan) / eq_value,
         "cpu_baseline": None,
         "cpu_baseline_note": "not timed for the served stream (hours of CPU work); see the bh1m workload",
     }
@@ -206,6 +251,12 @@ def run_batch(args, nb, torch):
     tune = b.tuning()
     b.close()
     seq = sequential_plain(nb, gals, eps2, dt, theta, threshold)
+    big = max(range(len(gals)), key=lambda g: gals[g][0].shape[0])
+    with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps2, theta=theta) as s:
+        s.init_soa(*gals[big])
+        plain_err = force_error(nb, s.compute_forces(), *gals[big], eps2)
+    th_eq, err_eq = plain_theta_for(nb, *gals[big], eps2)
+    seq_eq = sequential_plain(nb, gals, eps2, dt, th_eq, threshold)
     cpu = None if args.no_cpu_baseline else cpu_sample(gals, eps2, theta, threshold)
     return {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -214,9 +265,14 @@ def run_batch(args, nb, torch):
         "config": {"workload": "batch512", "galaxies": len(gals), "bodies": n_real,
                    "barnes_hut_members": len(bh_ids), "theta": theta, "eps": 0.01, "dt": dt,
                    "l2": "inputs (%.0f MB of state) larger than L2" % (n_real * 64 / 1e6)},
-        "sequential_plain": {"value": seq, "unit": METRIC,
+        "sequential_plain": {"value": seq, "unit": METRIC, "theta": theta,
+                             "force_rel_l2_vs_fp64_largest": plain_err,
                              "how": "one plain handle per galaxy, stepped one galaxy after another (2 steps each)"},
         "speedup_vs_sequential_plain": value / seq,
+        "sequential_plain_equal_accuracy": {
+            "value": seq_eq, "unit": METRIC, "theta": th_eq, "force_rel_l2_vs_fp64_largest": err_eq,
+            "how": "as sequential_plain, at the largest theta whose force error on the largest galaxy is <= 1e-3"},
+        "speedup_vs_sequential_plain_equal_accuracy": value / seq_eq,
         "force_rel_l2_vs_fp64_max": max(errs) if errs else None, "force_err_galaxies": len(errs),
         "interactions_per_step": info["interactions"], "tuning": tune,
         "e2e": {"value": n_real * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": n_real * 32,

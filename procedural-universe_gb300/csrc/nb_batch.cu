@@ -60,7 +60,7 @@ struct nb_batch {
     int* next_unit = nullptr;
     uint64_t direct_pairs = 0;
     // tuning and graph
-    nb_tuning tune{128, 1, 1024, 16, 128};
+    nb_tuning tune{128, 1, 1024, 32, 128};
     cudaGraphExec_t exec = nullptr;
     float graph_dt = NAN;
     bool graph_dirty = true;

@@ -496,10 +496,10 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             }
         }
     }
+    const float4 gb = gal_box[grp.x];
     // negated target coordinates, duplicated: the pair partner is the other list entry
     const float2 n0x = make_float2(-p0.x, -p0.x), n0y = make_float2(-p0.y, -p0.y), n0z = make_float2(-p0.z, -p0.z);
     const float2 n1x = make_float2(-p1.x, -p1.x), n1y = make_float2(-p1.y, -p1.y), n1z = make_float2(-p1.z, -p1.z);
-    const float4 gb = gal_box[grp.x];
     const float2 z2 = make_float2(0.f, 0.f);
     float2 a0x = z2, a0y = z2, a0z = z2, a1x = z2, a1y = z2, a1z = z2;   // (even entries, odd entries)
     float s0x = 0.f, s0y = 0.f, s0z = 0.f, c0x = 0.f, c0y = 0.f, c0z = 0.f;
@@ -647,6 +647,9 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             const int kind = mt.w & 15;
             count = __ldg(&cell_count[ch]);
             first = kind == BK_INTERNAL ? __ldg(&cell_first[ch]) : mt.x;
+            // The group form of the reference's rule side / r < theta: r is bounded
+            // below for every body of the group by the distance from the centre of
+            // mass to the group's bounding box.
             const int level = (int)__ldg(&cell_hi[ch]).w;
             const float side = ldexpf(gb.w, kSlotLevels - level);
             float d2 = 0.f;
