@@ -16,6 +16,16 @@ Workloads (seeded synthetic galaxies; no dataset is involved):
               eps=0.01, dt=1e-3
   direct4096  direct sum, N=4096 Plummer sphere, eps=0.01, dt=1e-3
 
+  batch512    512 galaxies, n log-uniform in [256, 65,536] (batched form)
+  served      Poisson stream of galaxy jobs, n log-uniform in [1,024, 1,048,576]
+              (served form: continuous batching under a memory budget)
+  bh1m_batched  the batched form (group traversal, quadrupoles) on the bh1m galaxy
+
+The default line (bh1m, one GPU) also carries "forms": the batched and the
+served form on their workloads, each against sequential plain-path launches
+at the plain path's own theta and at equal accuracy (force error <= 1e-3
+against the FP64 direct sum); --no-forms leaves them out.
+
 --impl reference times the reference's CPU algorithm (the oracle's
 restatement of BruteForceCPU / BarnesHut on all host cores) on the same
 workload, a bounded sample per step.
@@ -140,7 +150,10 @@ def measured_peaks():
 # --------------------------------------------------------------------------
 # CPU baseline: the reference's CPU algorithm (oracle restatement), bounded.
 # --------------------------------------------------------------------------
-def cpu_baseline(w, pm, v, budget_s=12.0):
+def cpu_baseline(w, pm, v, budget_s=12.0, F_gpu=None):
+    """Times the reference's algorithm (oracle restatement) on a bounded sample
+    of the workload; with F_gpu (the GPU forces of the same initial state) it
+    also reports their relative L2 difference on the sampled bodies."""
     from oracle import oracle as O
     threads = O.default_threads()
     cores = threads + 1                 # workers + the calling thread (CThreadPool layout)
@@ -156,7 +169,7 @@ def cpu_baseline(w, pm, v, budget_s=12.0):
         while True:
             targets = np.sort(rng.choice(n, m, replace=False))
             t0 = time.perf_counter()
-            tree.forces_subset(targets, G=1.0, S=S, theta=w["theta"])
+            Fo = tree.forces_subset(targets, G=1.0, S=S, theta=w["theta"])
             t_walk = time.perf_counter() - t0
             if t_walk > 2.0 or m >= n:
                 break
@@ -170,7 +183,7 @@ def cpu_baseline(w, pm, v, budget_s=12.0):
         while True:
             targets = np.sort(rng.choice(n, m, replace=False))
             t0 = time.perf_counter()
-            O.direct_forces_subset(rec, targets, G=1.0, S=S)
+            Fo = O.direct_forces_subset(rec, targets, G=1.0, S=S)
             t_f = time.perf_counter() - t0
             if t_f > min(2.0, budget_s) or m >= n:
                 break
@@ -178,8 +191,11 @@ def cpu_baseline(w, pm, v, budget_s=12.0):
         step_s = t_f * n / m
         sample = ("direct-sum forces of %d sampled target bodies against all %d sources on %d threads (%.2f s), "
                   "extrapolated to one step of %d bodies" % (m, n, threads, t_f, n))
-    return {"value": n / step_s, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample,
-            "step_s": step_s}
+    out = {"value": n / step_s, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample, "step_s": step_s}
+    if F_gpu is not None:
+        out["force_rel_l2_gpu_vs_port"] = float(O.rel_l2(F_gpu[targets], Fo))
+        out["force_compared_bodies"] = int(len(targets))
+    return out
 
 
 def run_reference(args, w):
@@ -224,6 +240,7 @@ def run_ours(args, w):
                       stream=stream.cuda_stream)
     rec_host = nb.records_from_soa(pm, v)
     sim.init(rec_host)
+    F_init = sim.compute_forces()      # forces of the initial state, compared with the CPU port below
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     dt = w["dt"]
 
@@ -275,28 +292,34 @@ def run_ours(args, w):
     value = world * n * args.steps / (total_ms * 1e-3)
 
     # ---- roofline of the dominant kernel ----
+    # Both kernels are bounded by FP32 arithmetic issue, not by HBM: the
+    # achieved figure is the interaction arithmetic (20 flops per interaction)
+    # per launch over the launch's average CUDA-event time, against the FP32
+    # FMA peak measured on this GPU.  The traversal's HBM side is reported
+    # beside it: its algorithmic bytes (body read + acceleration write, 32 B
+    # per body, plus one read of every tree cell) against the measured copy
+    # bandwidth.
     peaks, peak_src = measured_peaks()
+    fp32 = ctypes.c_double(0)
+    lib.nb_probe_fp32_peak(dev, ctypes.byref(fp32))
+    flops = FLOP_PER_INTERACTION * float(inter_last)
+    dom = "traverse" if w["kind"] == 2 else "direct_force"
+    ph = phases.get(dom, {})
+    t_launch = ph.get("ms_avg", float("nan")) * 1e-3
+    achieved = flops / t_launch / 1e12
+    roof = {"kernel": "k_traverse" if w["kind"] == 2 else "k_direct_force", "bound": "fp32", "achieved": achieved,
+            "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value if fp32.value else None,
+            "traffic": None, "peak_source": "measured on this GPU by an FMA-chain probe (nb_probe_fp32_peak)",
+            "flops_per_launch": flops, "interactions_per_launch": float(inter_last),
+            "launch_ms": t_launch * 1e3}
     if w["kind"] == 2:
-        dom = "traverse"
-        ph = phases.get(dom, {})
-        # algorithmic bytes per launch: body record read (16 B) + acceleration write (16 B) per body, plus one
-        # 16-B node/body record per interaction
-        alg_bytes = 32.0 * n + 16.0 * inter_last
-        achieved = alg_bytes / (ph.get("ms_avg", float("nan")) * 1e-3) / 1e9
-        roof = {"kernel": "k_traverse", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                "peak_source": peak_src + " hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes}
-    else:
-        dom = "direct_force"
-        ph = phases.get(dom, {})
-        fp32 = ctypes.c_double(0)
-        lib.nb_probe_fp32_peak(dev, ctypes.byref(fp32))
-        flops = FLOP_PER_INTERACTION * float(inter_last)
-        achieved = flops / (ph.get("ms_avg", float("nan")) * 1e-3) / 1e12
-        roof = {"kernel": "k_direct_force", "bound": "fp32", "achieved": achieved, "peak": fp32.value,
-                "unit": "TFLOP/s", "frac": achieved / fp32.value if fp32.value else None, "traffic": None,
-                "peak_source": "measured on this GPU by an FMA-chain probe (nb_probe_fp32_peak)",
-                "flops_per_launch": flops, "interactions_per_launch": float(inter_last)}
+        stats = sim.tree_stats()
+        alg_bytes = 32.0 * n + 48.0 * stats["nodes"]
+        roof["hbm"] = {"achieved": alg_bytes / t_launch / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                       "frac": alg_bytes / t_launch / 1e9 / peaks["hbm_gbs"], "peak_source": peak_src + " hbm_gbs",
+                       "algorithmic_bytes_per_launch": alg_bytes,
+                       "logical_node_bytes_per_launch": 16.0 * float(inter_last),
+                       "note": "the per-interaction node reads are served from L1/L2"}
 
     # ---- end-to-end through the C-ABI with pinned host records ----
     e2e = None
@@ -332,8 +355,11 @@ def run_ours(args, w):
         return 0
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(w, pm, v)
+        cpu = cpu_baseline(w, pm, v, F_gpu=F_init)
         cpu.pop("step_s", None)
+    forms = None
+    if world == 1 and not args.no_forms:
+        forms = run_forms(args)
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -348,6 +374,7 @@ def run_ours(args, w):
         "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)),
         "phases_ms_avg": {k: v_["ms_avg"] for k, v_ in phases.items()},
         "wall_s_timed_region": t_wall,
+        "forms": forms,
     }
     print(json.dumps(out))
     sim.close()
@@ -356,26 +383,65 @@ def run_ours(args, w):
     return 0
 
 
+def run_forms(args):
+    """The batched (512 galaxies) and served (Poisson stream) forms beside the
+    plain path, each against sequential plain launches: at the plain path's
+    own theta and at equal accuracy (force error <= 1e-3)."""
+    import torch
+    import nbody_gb300 as nb
+    import bench_forms
+
+    fargs = argparse.Namespace(steps=10, warmup=3, no_cpu_baseline=True)
+    out = {}
+    b = bench_forms.run_batch(fargs, nb, torch)
+    s = bench_forms.run_served(fargs, nb, torch)
+    for name, r in (("batch512", b), ("served", s)):
+        out[name] = {
+            "value": r["value"], "unit": r["unit"], "config": r["config"],
+            "force_rel_l2_vs_fp64": r.get("force_rel_l2_vs_fp64_max", r.get("force_rel_l2_vs_fp64_largest")),
+            "sequential_plain": {k: r["sequential_plain"][k] for k in
+                                 ("value", "theta", "force_rel_l2_vs_fp64_largest")},
+            "speedup_vs_sequential_plain": r["speedup_vs_sequential_plain"],
+            "sequential_plain_equal_accuracy": {k: r["sequential_plain_equal_accuracy"][k] for k in
+                                                ("value", "theta", "force_rel_l2_vs_fp64_largest")},
+            "speedup_vs_sequential_plain_equal_accuracy": r["speedup_vs_sequential_plain_equal_accuracy"],
+        }
+        for k in ("latency_s", "e2e", "tuning", "makespan_s"):
+            if r.get(k) is not None:
+                out[name][k] = r[k]
+    out["served"]["sequential_plain_equal_accuracy"]["latency_s"] = \
+        s["sequential_plain_equal_accuracy"]["latency_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bh1m", choices=sorted(WORKLOADS) + ["batch512", "served"])
+    ap.add_argument("--workload", default="bh1m", choices=sorted(WORKLOADS) + ["batch512", "served", "bh1m_batched"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched and served forms reported beside the plain-path line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     import nb_build
     nb_build.build()
-    if args.workload in ("batch512", "served"):
+    if args.workload in ("batch512", "served", "bh1m_batched"):
         import torch
         import nbody_gb300 as nb
         import bench_forms
         if dist_env()[1] != 0:
             return 0
-        fn = bench_forms.run_batch if args.workload == "batch512" else bench_forms.run_served
+        if args.impl == "reference":
+            if args.workload == "bh1m_batched":
+                return run_reference(args, WORKLOADS["bh1m"])
+            print(json.dumps(bench_forms.reference_line(args, nb, args.workload)))
+            return 0
+        fn = {"batch512": bench_forms.run_batch, "served": bench_forms.run_served,
+              "bh1m_batched": bench_forms.run_batch_single}[args.workload]
         print(json.dumps(fn(args, nb, torch)))
         return 0
     w = WORKLOADS[args.workload]

@@ -82,14 +82,19 @@ def sequential_plain(nb, gals, eps2, dt, theta, threshold, steps=2):
     return total_n / total_t
 
 
-def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7):
-    """The reference's CPU algorithms (oracle restatement) on a galaxy sample."""
+def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7, budget_s=20.0):
+    """The reference's CPU algorithms (oracle restatement) on a galaxy sample
+    (at most count galaxies, stopping once budget_s of CPU work is done)."""
     from oracle import oracle as O
     rng = np.random.default_rng(seed)
     pick = rng.choice(len(gals), min(count, len(gals)), replace=False)
     t_tot = 0.0
     n_tot = 0
+    done = []
     for g in pick:
+        if t_tot > budget_s:
+            break
+        done.append(g)
         pm, v = gals[g]
         rec = O.particles_from_soa(pm, v)
         t0 = time.perf_counter()
@@ -103,15 +108,40 @@ def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7):
         n_tot += pm.shape[0]
     return {"value": n_tot / t_tot, "unit": METRIC, "cores": O.default_threads() + 1, "kind": "port",
             "sample": "%d of the galaxies (%d bodies), one force pass each (Barnes-Hut per-body rule at theta=%.1f "
-                      "for n >= %d, direct sum below) on all host cores" % (len(pick), n_tot, theta, threshold)}
+                      "for n >= %d, direct sum below) on all host cores" % (len(done), n_tot, theta, threshold)}
 
 
-def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
-    import nbody_serve as ns
+def served_stream(requests=48, rate=200.0):
+    """Seeded Poisson arrivals and log-uniform job sizes in [1,024, 1,048,576]."""
     rng = np.random.default_rng(5)
     gaps = rng.exponential(1.0 / rate, requests)
     arrivals = np.cumsum(gaps) - gaps[0]
     sizes = np.round(np.exp(rng.uniform(np.log(1024), np.log(1 << 20), requests))).astype(int)
+    return arrivals, sizes
+
+
+def reference_line(args, nb, workload):
+    """The reference's CPU algorithms (oracle restatement) on a bounded sample
+    of the batched or served workload, as the reference arm's JSON line."""
+    if workload == "batch512":
+        gals = batch_galaxies(nb)
+        cpu = cpu_sample(gals, 1e-4, 0.6, 8192)
+        cfg = {"workload": "batch512", "galaxies": len(gals)}
+    else:
+        _, sizes = served_stream()
+        gals = [nb.seed_disk(10_000 + k, int(n)) for k, n in enumerate(sizes)]
+        cpu = cpu_sample(gals, 0.005 ** 2, 0.5, 1024, count=len(gals))
+        cfg = {"workload": "served", "requests": len(sizes)}
+    return {"metric": METRIC, "value": cpu["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)", "config": cfg,
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
+    import nbody_serve as ns
+    arrivals, sizes = served_stream(requests, rate)
     server = ns.NBodyServer(max_active=64, steps_per_round=25, bh_threshold=1024, softening2=eps * eps, theta=theta)
     ids = []
     submitted = 0
@@ -193,6 +223,53 @@ def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, the
         "speedup_vs_sequential_plain_equal_accuracy": (total / makespan) / eq_value,
         "cpu_baseline": None,
         "cpu_baseline_note": "not timed for the served stream (hours of CPU work); see the bh1m workload",
+    }
+
+
+def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
+    """The batched form on the 1M-body disk + bulge galaxy of the plain-path
+    workload: the same galaxy, theta and softening, stepped by the group-wise
+    traversal with quadrupoles from a CUDA graph."""
+    eps2 = eps * eps
+    pm, v = nb.seed_disk(1234, n)
+    stream = torch.cuda.Stream()
+    b = nb.NBodyBatch(bh_threshold=1024, bh_theta=theta, softening2=eps2, stream=stream.cuda_stream)
+    b.add(pm, v)
+    b.commit()
+    err = force_error(nb, b.forces(0), pm, v, eps2)
+    b.step(dt, args.warmup)
+    flush = torch.empty((512 << 20) // 4, dtype=torch.float32, device="cuda")
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            b.step(dt, 1)
+            evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(sum(a.elapsed_time(c) for a, c in evs)) / args.steps
+    info = b.info()
+    stats = b.tree_stats()
+    b.close()
+    plain = sequential_plain(nb, [(pm, v)], eps2, dt, theta, 2)
+    with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps2, theta=theta) as s:
+        s.init_soa(pm, v)
+        plain_err = force_error(nb, s.compute_forces(), pm, v, eps2)
+    th_eq, err_eq = plain_theta_for(nb, pm, v, eps2)
+    plain_eq = sequential_plain(nb, [(pm, v)], eps2, dt, th_eq, 2)
+    return {
+        "metric": METRIC, "value": n / (ms * 1e-3), "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxy)",
+        "config": {"workload": "bh1m_batched", "n": n, "theta": theta, "eps": eps, "dt": dt,
+                   "l2": "flushed (512 MB write) before every timed step"},
+        "force_rel_l2_vs_fp64": err, "interactions_per_body": info["interactions"] / n,
+        "groups": stats["groups"], "bodies_per_group": n / max(1, stats["groups"]),
+        "plain": {"value": plain, "theta": theta, "force_rel_l2_vs_fp64": plain_err},
+        "plain_equal_accuracy": {"value": plain_eq, "theta": th_eq, "force_rel_l2_vs_fp64": err_eq},
+        "speedup_vs_plain": n / (ms * 1e-3) / plain,
+        "speedup_vs_plain_equal_accuracy": n / (ms * 1e-3) / plain_eq,
     }
 
 

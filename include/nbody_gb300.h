@@ -277,7 +277,8 @@ void* nb_batch_stream(nb_batch* b);
 
 /* ---- served form: continuous batching of galaxy jobs ---------------------- */
 /* Jobs arrive, wait in a FIFO queue, are admitted while the estimated device
- * bytes of the active jobs (about 170 bytes per body: state, tree, scratch)
+ * bytes of the active jobs (640 bytes per body: state, sort and topology
+ * scratch, tree cells with quadrupoles at twice their measured count)
  * stay within memory_budget and a slot is free, and are stepped together in
  * rounds by the batched form; a round takes at most steps_per_round steps and
  * never more than the nearest job completion, so that finished jobs leave and

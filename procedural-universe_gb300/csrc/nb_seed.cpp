@@ -19,7 +19,7 @@
 //
 // The reference's own seeders (src/Sim/RandomSeeder.cpp:12-40,
 // src/Sim/GalaxySeeder.cpp:43-144, src/Sim/StarSystemSeeder.cpp:17-55) are
-// restated in nb_seed_reference with the same distributions; their random
+// restated in nb_seed_reference (nb_io.cpp) with the same distributions; their random
 // streams cannot match (std::default_random_engine is implementation-defined).
 #include "nb_rng.hpp"
 #include "../../include/nbody_gb300.h"
