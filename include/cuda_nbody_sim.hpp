@@ -78,6 +78,19 @@ class CudaNBodySim : public INBodySim {
         return v;
     }
 
+    // Device vertex buffer (LWParticle layout) that every following Update
+    // fills in the kick-drift's epilogue, coloured from the records; valid
+    // until the next Init.
+    void* AttachRenderBuffer(float scale = 1.0f) {
+        if (!particles_) throw std::runtime_error("AttachRenderBuffer before Init");
+        std::vector<float> colour(4 * particles_->size());
+        for (size_t i = 0; i < particles_->size(); ++i)
+            for (int k = 0; k < 4; ++k) colour[4 * i + k] = (*particles_)[i].colour[k];
+        void* dev = nullptr;
+        check(nb_render_attach(sim_, colour.data(), scale, &dev), "nb_render_attach");
+        return dev;
+    }
+
     // Octree of the current positions (Barnes-Hut), for debug drawing.
     std::vector<nb_tree_node> TreeNodes() {
         size_t n = 0;

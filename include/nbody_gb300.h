@@ -133,6 +133,13 @@ int  nb_init_particles(nb_sim* sim, const nb_particle* particles, size_t n);
 /* Same from structure-of-arrays host buffers: pos_mass = n x (x,y,z,m),
  * vel = n x (vx,vy,vz,unused). */
 int  nb_init_soa(nb_sim* sim, const float* pos_mass4, const float* vel4, size_t n);
+/* A reference seeder run on the GPU, then Init: the seeder's
+ * Seed(particles) followed by Init(particles) (src/Sim/IParticleSeeder.hpp:12-50,
+ * src/States/Simulation/SimulationState.cpp:167-171) without host records.
+ * seeder 0 = RandomSeeder, 1 = GalaxySeeder, 2 = StarSystemSeeder (same
+ * distributions and bodies as nb_seed_reference); records_out (n records,
+ * may be null) receives the generated records. */
+int  nb_init_seeded(nb_sim* sim, int seeder, uint64_t seed, float scale, size_t n, nb_particle* records_out);
 size_t nb_count(const nb_sim* sim);
 
 /* INBodySim::Update(dt) (src/Sim/BruteForceCPU.cpp:45-74, src/Sim/BarnesHut.cpp:44-96):
@@ -354,6 +361,16 @@ int  nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* accel4, do
 /* Headless render hand-off: fills n render vertices (LWParticle) with the
  * current positions and the given per-body colour (n x float4) and scale. */
 int  nb_render_vertices(nb_sim* sim, const float* colour4, float scale, nb_render_vertex* out, size_t n);
+/* Render hand-off without the per-frame copy of the records
+ * (src/States/Simulation/SimulationState.cpp:57-60, 88-103): attaches a device
+ * buffer of n vertices (colour4: n x float4 host colours, null for white) that
+ * every following kick-drift fills in its epilogue with the moved positions.
+ * *device_vertices stays valid until nb_render_detach, the next nb_init_* or
+ * nb_destroy; a renderer binds it directly (e.g. through graphics interop or
+ * a device copy). nb_render_read copies it to the host. */
+int  nb_render_attach(nb_sim* sim, const float* colour4, float scale, void** device_vertices);
+int  nb_render_detach(nb_sim* sim);
+int  nb_render_read(nb_sim* sim, nb_render_vertex* out, size_t n);
 
 /* ---- initial conditions (seeders) ---------------------------------------- */
 /* Counter-based seeded generators. Output: n x (x,y,z,m) and n x (vx,vy,vz,0),

@@ -7,6 +7,7 @@
 // per handle (nb_last_error).
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
+#include "nb_refseed.hpp"
 #include <cmath>
 #include <cstring>
 #include <cstdio>
@@ -125,7 +126,15 @@ __global__ void k_render_fill(const float4* __restrict__ pos, const float4* __re
     out[i] = v;
 }
 
+void detach_render(nb_sim* s) {
+    cudaFree(s->render);
+    cudaFree(s->rcolour);
+    s->render = nullptr;
+    s->rcolour = nullptr;
+}
+
 void free_state(nb_sim* s) {
+    detach_render(s);
     cudaFree(s->pos); cudaFree(s->posc); cudaFree(s->vel); cudaFree(s->velc); cudaFree(s->acc);
     cudaFree(s->finit); cudaFree(s->part);
     s->pos = s->posc = s->vel = s->velc = s->acc = s->finit = s->part = nullptr;
@@ -135,6 +144,7 @@ void free_state(nb_sim* s) {
 }
 
 int ensure_state(nb_sim* s, size_t n) {
+    detach_render(s);   // a new particle set invalidates the vertex buffer (re-attach after Init)
     const size_t n_pad = pad_up(std::max<size_t>(n, 1), kPad);
     if (n_pad > s->cap) {
         free_state(s);
@@ -302,9 +312,27 @@ size_t nb_count(const nb_sim* s) { return s ? s->n : 0; }
 
 void* nb_stream(nb_sim* s) { return s ? (void*)s->stream : nullptr; }
 
-int nb_init_particles(nb_sim* s, const nb_particle* particles, size_t n) {
-    if (!s) return NB_EINVAL;
-    if (!particles && n) return fail(s, NB_EINVAL, "null particle buffer");
+}  // extern "C"
+
+namespace {
+
+// Fills the records on the device: from the caller's host records (seeder < 0)
+// or from one of the reference's seeders run on the GPU.
+__global__ void k_seed_records(int seeder, uint64_t seed, float scale, nb::refseed::GalaxyFrame frame, int n,
+                               nb_particle* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    nb_particle p;
+    if (seeder == 0) nb::refseed::random_body(seed, (size_t)i, scale, p);
+    else if (seeder == 1) nb::refseed::galaxy_body(seed, (size_t)i, scale, frame, p);
+    else nb::refseed::star_system_body(seed, (size_t)i, p);
+    out[i] = p;
+}
+
+// nb_init_particles / nb_init_seeded: records in host memory (host != null)
+// or generated on the device, unpacked into the simulator's state.
+int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, float scale, size_t n,
+                 nb_particle* records_out) {
     if (n > (size_t)INT32_MAX - kPad) return fail(s, NB_EINVAL, "too many particles");
     cudaSetDevice(s->dev);
     int rc = ensure_state(s, n);
@@ -314,7 +342,16 @@ int nb_init_particles(nb_sim* s, const nb_particle* particles, size_t n) {
     int* d_any = nullptr;
     NB_CUDA(s, cudaMallocAsync(&d_rec, n * sizeof(nb_particle) + 16, s->stream));
     d_any = (int*)((char*)d_rec + n * sizeof(nb_particle));
-    cudaError_t e = cudaMemcpyAsync(d_rec, particles, n * sizeof(nb_particle), cudaMemcpyHostToDevice, s->stream);
+    cudaError_t e = cudaSuccess;
+    if (host) {
+        e = cudaMemcpyAsync(d_rec, host, n * sizeof(nb_particle), cudaMemcpyHostToDevice, s->stream);
+    } else {
+        const nb::refseed::GalaxyFrame frame = nb::refseed::galaxy_frame(seed, n);
+        k_seed_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(seeder, seed, scale, frame, (int)n, d_rec);
+        e = cudaGetLastError();
+        if (e == cudaSuccess && records_out)
+            e = cudaMemcpyAsync(records_out, d_rec, n * sizeof(nb_particle), cudaMemcpyDeviceToHost, s->stream);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(d_any, 0, sizeof(int), s->stream);
     if (e == cudaSuccess) {
         k_unpack_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(d_rec, (int)n, s->prm.kind, s->pos,
@@ -327,11 +364,27 @@ int nb_init_particles(nb_sim* s, const nb_particle* particles, size_t n) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) any = *s->h_err;
     cudaFreeAsync(d_rec, s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_init_particles");
+    if (e != cudaSuccess) return cuda_fail(s, e, host ? "nb_init_particles" : "nb_init_seeded");
     s->finit_pending = any != 0;
     rc = check_device_error(s);
     if (rc) { s->n = 0; return rc; }
     return NB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nb_init_particles(nb_sim* s, const nb_particle* particles, size_t n) {
+    if (!s) return NB_EINVAL;
+    if (!particles && n) return fail(s, NB_EINVAL, "null particle buffer");
+    return init_records(s, particles, -1, 0, 1.f, n, nullptr);
+}
+
+int nb_init_seeded(nb_sim* s, int seeder, uint64_t seed, float scale, size_t n, nb_particle* records_out) {
+    if (!s) return NB_EINVAL;
+    if (seeder < 0 || seeder > 2 || !(scale > 0)) return fail(s, NB_EINVAL, "bad seeder or scale");
+    return init_records(s, nullptr, seeder, seed, scale, n, records_out);
 }
 
 int nb_init_soa(nb_sim* s, const float* pos_mass4, const float* vel4, size_t n) {
@@ -534,6 +587,56 @@ int nb_render_vertices(nb_sim* s, const float* colour4, float scale, nb_render_v
     cudaFreeAsync(d_v, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_fail(s, e, "nb_render_vertices");
+    return NB_OK;
+}
+
+int nb_render_attach(nb_sim* s, const float* colour4, float scale, void** device_vertices) {
+    if (!s || !device_vertices) return NB_EINVAL;
+    if (s->n == 0) return fail(s, NB_EBADSTATE, "nb_init_* first");
+    cudaSetDevice(s->dev);
+    detach_render(s);
+    const size_t n = s->n;
+    NB_CUDA(s, cudaMalloc(&s->render, n * sizeof(nb_render_vertex)));
+    cudaError_t e = cudaMalloc(&s->rcolour, n * sizeof(float4));
+    if (e == cudaSuccess) {
+        if (colour4) {
+            e = cudaMemcpyAsync(s->rcolour, colour4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+        } else {
+            std::vector<float4> white(n, make_float4(1.f, 1.f, 1.f, 1.f));
+            e = cudaMemcpyAsync(s->rcolour, white.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);   // before `white` goes away
+        }
+    }
+    if (e == cudaSuccess) {
+        s->rscale = scale;
+        k_render_fill<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->rcolour, scale, (int)n,
+                                                                         s->render);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) {
+        detach_render(s);
+        return cuda_fail(s, e, "nb_render_attach");
+    }
+    *device_vertices = s->render;
+    return NB_OK;
+}
+
+int nb_render_detach(nb_sim* s) {
+    if (!s) return NB_EINVAL;
+    cudaSetDevice(s->dev);
+    cudaStreamSynchronize(s->stream);
+    detach_render(s);
+    return NB_OK;
+}
+
+int nb_render_read(nb_sim* s, nb_render_vertex* out, size_t n) {
+    if (!s || (!out && n)) return NB_EINVAL;
+    if (!s->render) return fail(s, NB_EBADSTATE, "no vertex buffer attached");
+    if (n != s->n) return fail(s, NB_EINVAL, "vertex count differs from the initialised count");
+    cudaSetDevice(s->dev);
+    NB_CUDA(s, cudaMemcpyAsync(out, s->render, n * sizeof(nb_render_vertex), cudaMemcpyDeviceToHost, s->stream));
+    NB_CUDA(s, cudaStreamSynchronize(s->stream));
     return NB_OK;
 }
 

@@ -8,9 +8,10 @@
 //    level-7 nodes are the galaxy roots.
 //  * The mass pass adds traceless quadrupole moments (parallel-axis rule
 //    bottom-up).  Traversal groups are taken from the tree itself: the
-//    largest subtrees of at most kGroupMax bodies, consecutive small siblings
-//    packed together, oversized depth-cap buckets cut into chunks -- so a
-//    group is spatially compact and its bounding box small.  A warp takes
+//    largest subtrees of at most kGroupMax bodies whose cell is at most
+//    1/16 of the galaxy cube, consecutive small siblings packed together,
+//    oversized depth-cap buckets cut into chunks -- so a group is spatially
+//    compact and its bounding box small.  A warp takes
 //    groups from a device queue (two bodies per lane), opens a cell when the
 //    cell side exceeds theta times the distance from the cell's centre of
 //    mass to the group's bounding box, and collects accepted cells (monopole
@@ -31,6 +32,7 @@ constexpr int kMortonLevels = 14;       // 42 bits of position in the galaxy cub
 constexpr int kBatchDepth = kSlotLevels + kMortonLevels;
 constexpr int kGWarps = 4;              // warps per traversal block
 constexpr int kGroupMax = 64;           // bodies per traversal group (two per lane)
+constexpr int kGroupMinDepth = 4;       // a group cell lies >= 4 levels below its galaxy root
 constexpr int kBoxChunk = 8192;         // bodies per block of the bounding-box pass
 constexpr int kGStack = 512;            // cells waiting to be opened, per warp (<= 32 pushed per step)
 constexpr int kGCells = 64;             // accepted-cell list, per warp
@@ -319,11 +321,14 @@ __device__ __forceinline__ void cell_accel(const float4 p, const float4 cm, cons
 }
 
 // ---- traversal groups from the tree --------------------------------------------
-// One thread per internal node at or below the galaxy roots.  A node with more
-// than kGroupMax bodies packs its consecutive children of at most kGroupMax
-// bodies into groups (children are contiguous in sorted order) and cuts a
-// larger depth-cap bucket into chunks; a galaxy root of at most kGroupMax
-// bodies is one group.  Every body lands in exactly one group.
+// One thread per internal node at or below the galaxy roots.  A node that
+// cannot be a group itself emits its children that can (packing consecutive
+// ones, children being contiguous in sorted order, when the node is deep
+// enough), emits a body that sits high in the tree on its own and cuts a
+// larger depth-cap bucket into chunks; internal children that cannot be
+// groups are handled by their own threads.  Every body lands in exactly one
+// group: the first groupable cell on its path from the galaxy root, or its
+// leaf.
 __device__ __forceinline__ void emit_group(int first, int count, const int32_t* sorder, const int32_t* body_slot,
                                            int nbodies, int4* groups, int cap, int* n_groups, int* err) {
     if (count <= 0) return;
@@ -337,6 +342,15 @@ __device__ __forceinline__ void emit_group(int first, int count, const int32_t* 
         return;
     }
     groups[idx] = make_int4(body_slot[sorder[first]], first, count, 0);
+}
+
+// A cell can be a group when it holds at most kGroupMax bodies and lies at
+// least kGroupMinDepth levels below its galaxy's root (side <= cube / 16): a
+// few bodies spread over a large, sparse cell would give one group a box the
+// size of the galaxy and a list of ~10^5 entries (a tail that held one warp
+// for milliseconds); such cells are split further instead.
+__device__ __forceinline__ bool groupable(int level, int count) {
+    return count <= kGroupMax && level >= kSlotLevels + kGroupMinDepth;
 }
 
 __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_dev, const int32_t* __restrict__ int_cell,
@@ -355,16 +369,15 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
     const int level = (int)cell_hi[c].w;
     const int cnt = cell_count[c];
     if (level < kSlotLevels) return;
-    if (cnt <= kGroupMax) {
-        if (level == kSlotLevels) emit_group(cell_first[c], cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
-        return;   // otherwise an ancestor groups it
-    }
+    if (groupable(level, cnt)) return;   // its parent groups it
     const int4 pm = cell_meta[c];
     const int F = pm.x, nch = (pm.w >> 4) & 15;
     if (F < 1 || nch > 8 || F + nch > n_cells) {
         record_error(err, DEV_TREE_OVERFLOW);
         return;
     }
+    // siblings are packed only below a cell small enough to be a group itself
+    const bool pack = level >= kSlotLevels + kGroupMinDepth;
     int run_first = -1, run_cnt = 0;
     for (int j = 0; j < nch; ++j) {
         const int ch = F + j;
@@ -372,14 +385,18 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
         const int kind = mt.w & 15;
         const int cc = cell_count[ch];
         const int cf = kind == BK_INTERNAL ? cell_first[ch] : mt.x;
-        if (cc > kGroupMax) {
+        if (!groupable((int)cell_hi[ch].w, cc)) {
             emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
             run_first = -1;
             run_cnt = 0;
-            if (kind != BK_INTERNAL)   // an oversized depth-cap bucket
+            if (kind != BK_INTERNAL)   // a body high in the tree, or an oversized depth-cap bucket
                 for (int o = 0; o < cc; o += kGroupMax)
                     emit_group(cf + o, min(kGroupMax, cc - o), sorder, body_slot, nbodies, groups, cap, n_groups, err);
             continue;                  // an internal child groups its own children
+        }
+        if (!pack) {
+            emit_group(cf, cc, sorder, body_slot, nbodies, groups, cap, n_groups, err);
+            continue;
         }
         if (run_cnt + cc > kGroupMax) {
             emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);

@@ -155,11 +155,22 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
 // pending initial forces, store the acceleration and, when update != 0,
 // kick-drift: v += a dt; x += v dt / scale, both Kahan-compensated
 // (src/Sim/BruteForceCPU.cpp:61-73).
+// Render hand-off in the update's epilogue: the vertex (LWParticle layout,
+// 32 bytes) of a body the update just moved, as two 16-byte stores.
+__device__ __forceinline__ void write_vertex(nb_render_vertex* rv, const float4* rcol, float rscale, int i,
+                                             const float4 x) {
+    const float4 c = rcol[i];
+    float4* o = reinterpret_cast<float4*>(rv + i);
+    o[0] = make_float4(x.x, x.y, x.z, c.x);
+    o[1] = make_float4(c.y, c.z, c.w, rscale);
+}
+
 __global__ void k_direct_reduce_update(const float4* __restrict__ part, int splits, int n, int n_pad, float G,
                                        const float4* __restrict__ finit, float4* __restrict__ acc,
                                        float4* __restrict__ pos, float4* __restrict__ posc,
                                        float4* __restrict__ vel, float4* __restrict__ velc, float dt,
-                                       float inv_scale, int update, int comp) {
+                                       float inv_scale, int update, int comp, nb_render_vertex* __restrict__ rv,
+                                       const float4* __restrict__ rcol, float rscale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
@@ -194,13 +205,15 @@ __global__ void k_direct_reduce_update(const float4* __restrict__ part, int spli
     }
     vel[i] = v;
     pos[i] = x;
+    if (rv) write_vertex(rv, rcol, rscale, i, x);
 }
 
 // Kick-drift from a stored acceleration (Barnes-Hut path,
 // src/Sim/BarnesHut.cpp:81-95).
 __global__ void k_kick_drift(const float4* __restrict__ acc, int n, float4* __restrict__ pos,
                              float4* __restrict__ posc, float4* __restrict__ vel, float4* __restrict__ velc,
-                             float dt, float inv_scale, int comp) {
+                             float dt, float inv_scale, int comp, nb_render_vertex* __restrict__ rv,
+                             const float4* __restrict__ rcol, float rscale) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 a = acc[i];
@@ -220,6 +233,7 @@ __global__ void k_kick_drift(const float4* __restrict__ acc, int n, float4* __re
     }
     vel[i] = v;
     pos[i] = x;
+    if (rv) write_vertex(rv, rcol, rscale, i, x);
 }
 
 namespace {
@@ -324,7 +338,8 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     PhaseScope ps(sim, 1);
     k_direct_reduce_update<<<(n + 255) / 256, 256, 0, sim->stream>>>(
         sim->part, splits, n, (int)sim->n_pad, (float)sim->prm.G, sim->finit_pending ? sim->finit : nullptr,
-        sim->acc, sim->pos, sim->posc, sim->vel, sim->velc, dt, inv_scale, update ? 1 : 0, comp ? 1 : 0);
+        sim->acc, sim->pos, sim->posc, sim->vel, sim->velc, dt, inv_scale, update ? 1 : 0, comp ? 1 : 0,
+        update ? sim->render : nullptr, sim->rcolour, sim->rscale);
     sim->finit_pending = false;
     const double nn = (double)sim->n;
     sim->inter_last = (uint64_t)(nn * (nn - 1.0));
@@ -336,7 +351,8 @@ cudaError_t kick_drift(nb_sim* sim, float dt) {
     const bool comp = !(sim->prm.flags & NB_FLAG_NO_COMPENSATION);
     PhaseScope ps(sim, 7);
     k_kick_drift<<<(n + 255) / 256, 256, 0, sim->stream>>>(sim->acc, n, sim->pos, sim->posc, sim->vel, sim->velc,
-                                                           dt, (float)(1.0 / sim->prm.pos_scale), comp ? 1 : 0);
+                                                           dt, (float)(1.0 / sim->prm.pos_scale), comp ? 1 : 0,
+                                                           sim->render, sim->rcolour, sim->rscale);
     return cudaGetLastError();
 }
 

@@ -130,6 +130,11 @@ struct nb_sim {
     float4* acc = nullptr;    // acceleration of the last force evaluation (G applied)
     float4* finit = nullptr;  // initial forces / m from the records, applied once (direct sum)
     bool finit_pending = false;
+    // render hand-off: when attached, every kick-drift also writes the vertex
+    // (position, colour, scale) of each body it moves
+    nb_render_vertex* render = nullptr;
+    float4* rcolour = nullptr;
+    float rscale = 1.f;
     // direct-sum partial sums
     float4* part = nullptr;   // [splits][n_pad] sums then [splits][n_pad] compensations
     size_t part_cap = 0;      // in float4 entries

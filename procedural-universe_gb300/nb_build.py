@@ -38,7 +38,10 @@ def up_to_date() -> bool:
 
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    # host code: no contraction into fused multiply-adds, so that host results
+    # (seeders, file re-centring) are the same on x86-64 and AArch64
     cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
     if verbose_ptxas and src.endswith(".cu"):
         cmd[1:1] = ["-Xptxas", "-v"]

@@ -140,6 +140,10 @@ def lib() -> ctypes.CDLL:
             "nb_seed_disk": ([ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp], i32),
             "nb_seed_collision": ([ctypes.c_uint64, sz, f64, f64, f64, vp, vp], i32),
             "nb_seed_reference": ([i32, ctypes.c_uint64, f32, vp, sz], i32),
+            "nb_init_seeded": ([vp, i32, ctypes.c_uint64, f32, sz, vp], i32),
+            "nb_render_attach": ([vp, vp, f32, vp], i32),
+            "nb_render_detach": ([vp], i32),
+            "nb_render_read": ([vp, vp, sz], i32),
             "nb_file_write": ([ctypes.c_char_p, vp, sz], i32),
             "nb_file_read": ([ctypes.c_char_p, vp, sz, vp, i32], i32),
         }
@@ -290,6 +294,13 @@ class NBodySim:
         self._check(lib().nb_init_particles(self._h, _ptr(p), p.shape[0]), "nb_init_particles")
         self.n = p.shape[0]
 
+    def init_seeded(self, seeder: int, seed: int, n: int, scale: float = 1.0) -> np.ndarray:
+        """A reference seeder run on the GPU, then Init; returns the generated records."""
+        p = np.zeros(n, dtype=PARTICLE_DTYPE)
+        self._check(lib().nb_init_seeded(self._h, seeder, seed, scale, n, _ptr(p)), "nb_init_seeded")
+        self.n = n
+        return p
+
     def init_soa(self, pos_mass: np.ndarray, vel: np.ndarray):
         pm = np.ascontiguousarray(pos_mass, np.float32)
         v = np.ascontiguousarray(vel, np.float32)
@@ -380,6 +391,21 @@ class NBodySim:
         out = np.zeros(self.n, RENDER_DTYPE)
         c = None if colour is None else np.ascontiguousarray(colour, np.float32)
         self._check(lib().nb_render_vertices(self._h, _ptr(c), scale, _ptr(out), self.n), "nb_render_vertices")
+        return out
+
+    def render_attach(self, colour: np.ndarray | None = None, scale: float = 1.0) -> int:
+        """Attaches the device vertex buffer filled by every kick-drift; returns its device address."""
+        c = None if colour is None else np.ascontiguousarray(colour, np.float32)
+        ptr = ctypes.c_void_p()
+        self._check(lib().nb_render_attach(self._h, _ptr(c), scale, ctypes.byref(ptr)), "nb_render_attach")
+        return ptr.value
+
+    def render_detach(self):
+        self._check(lib().nb_render_detach(self._h), "nb_render_detach")
+
+    def render_read(self) -> np.ndarray:
+        out = np.zeros(self.n, RENDER_DTYPE)
+        self._check(lib().nb_render_read(self._h, _ptr(out), self.n), "nb_render_read")
         return out
 
 
