@@ -126,6 +126,39 @@ __global__ void k_render_fill(const float4* __restrict__ pos, const float4* __re
     out[i] = v;
 }
 
+// Device / pinned host staging of at least `bytes`, reused across calls.
+void* device_stage(nb_sim* s, size_t bytes) {
+    if (bytes > s->d_stage_bytes) {
+        cudaStreamSynchronize(s->stream);
+        cudaFree(s->d_stage);
+        s->d_stage = nullptr;
+        s->d_stage_bytes = 0;
+        if (cudaMalloc(&s->d_stage, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            s->d_stage = nullptr;
+            return nullptr;
+        }
+        s->d_stage_bytes = bytes;
+    }
+    return s->d_stage;
+}
+
+void* host_stage(nb_sim* s, size_t bytes) {
+    if (bytes > s->h_stage_bytes) {
+        cudaStreamSynchronize(s->stream);
+        if (s->h_stage) cudaFreeHost(s->h_stage);
+        s->h_stage = nullptr;
+        s->h_stage_bytes = 0;
+        if (cudaMallocHost(&s->h_stage, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            s->h_stage = nullptr;
+            return nullptr;
+        }
+        s->h_stage_bytes = bytes;
+    }
+    return s->h_stage;
+}
+
 void detach_render(nb_sim* s) {
     cudaFree(s->render);
     cudaFree(s->rcolour);
@@ -295,6 +328,8 @@ int nb_destroy(nb_sim* s) {
     cudaSetDevice(s->dev);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_state(s);
+    cudaFree(s->d_stage);
+    if (s->h_stage) cudaFreeHost(s->h_stage);
     for (auto& p : s->prof.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (cudaEvent_t e : s->prof.pool) cudaEventDestroy(e);
     cudaFree(s->dscratch);
@@ -338,10 +373,9 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
     int rc = ensure_state(s, n);
     if (rc) return rc;
     if (n == 0) return NB_OK;
-    nb_particle* d_rec = nullptr;
-    int* d_any = nullptr;
-    NB_CUDA(s, cudaMallocAsync(&d_rec, n * sizeof(nb_particle) + 16, s->stream));
-    d_any = (int*)((char*)d_rec + n * sizeof(nb_particle));
+    nb_particle* d_rec = static_cast<nb_particle*>(device_stage(s, n * sizeof(nb_particle) + 16));
+    if (!d_rec) return fail(s, NB_ENOMEM, "device staging allocation failed");
+    int* d_any = (int*)((char*)d_rec + n * sizeof(nb_particle));
     cudaError_t e = cudaSuccess;
     if (host) {
         e = cudaMemcpyAsync(d_rec, host, n * sizeof(nb_particle), cudaMemcpyHostToDevice, s->stream);
@@ -363,7 +397,6 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, d_any, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e == cudaSuccess) any = *s->h_err;
-    cudaFreeAsync(d_rec, s->stream);
     if (e != cudaSuccess) return cuda_fail(s, e, host ? "nb_init_particles" : "nb_init_seeded");
     s->finit_pending = any != 0;
     rc = check_device_error(s);
@@ -427,14 +460,13 @@ int nb_read_state(nb_sim* s, float* pos3, double* vel3, double* force3) {
     cudaSetDevice(s->dev);
     const size_t n = s->n;
     if (n == 0) return NB_OK;
-    WbRecord* d_wb = nullptr;
-    NB_CUDA(s, cudaMallocAsync(&d_wb, n * sizeof(WbRecord), s->stream));
+    WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
+    WbRecord* h = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
+    if (!d_wb || !h) return fail(s, NB_ENOMEM, "staging allocation failed");
     k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
                                                                         (int)n, 0, d_wb);
-    std::vector<WbRecord> h(n);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(d_wb, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return cuda_fail(s, e, "nb_read_state");
     int rc = check_device_error(s);
@@ -453,21 +485,18 @@ int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
     if (n == 0) return NB_OK;
     if (!particles) return fail(s, NB_EINVAL, "null particle buffer");
     cudaSetDevice(s->dev);
-    WbRecord* d_wb = nullptr;
-    WbRecord* h_wb = nullptr;
-    NB_CUDA(s, cudaMallocAsync(&d_wb, n * sizeof(WbRecord), s->stream));
-    cudaError_t e = cudaMallocHost(&h_wb, n * sizeof(WbRecord));
-    if (e != cudaSuccess) { cudaFreeAsync(d_wb, s->stream); return cuda_fail(s, e, "cudaMallocHost"); }
+    WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
+    WbRecord* h_wb = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
+    if (!d_wb || !h_wb) return fail(s, NB_ENOMEM, "staging allocation failed");
     const int zero = (s->prm.kind != NB_SIM_BARNES_HUT) && !s->forces_fresh;
     k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
                                                                         (int)n, zero, d_wb);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_wb, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(d_wb, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) { cudaFreeHost(h_wb); return cuda_fail(s, e, "nb_write_back"); }
+    if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
     int rc = check_device_error(s);
-    if (rc) { cudaFreeHost(h_wb); return rc; }
+    if (rc) return rc;
     auto scatter = [&](size_t b, size_t end) {
         for (size_t i = b; i < end; ++i) {
             nb_particle& p = particles[i];
@@ -490,7 +519,6 @@ int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
     } else {
         scatter(0, n);
     }
-    cudaFreeHost(h_wb);
     return NB_OK;
 }
 

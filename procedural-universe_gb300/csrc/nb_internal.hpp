@@ -135,6 +135,13 @@ struct nb_sim {
     nb_render_vertex* render = nullptr;
     float4* rcolour = nullptr;
     float rscale = 1.f;
+    // staging of the record boundary (nb_init_particles, nb_write_back,
+    // nb_read_state): grown on demand and kept, so that a step through the
+    // C-ABI allocates nothing
+    void* d_stage = nullptr;
+    size_t d_stage_bytes = 0;
+    void* h_stage = nullptr;   // pinned
+    size_t h_stage_bytes = 0;
     // direct-sum partial sums
     float4* part = nullptr;   // [splits][n_pad] sums then [splits][n_pad] compensations
     size_t part_cap = 0;      // in float4 entries
