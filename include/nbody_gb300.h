@@ -100,6 +100,11 @@ typedef struct nb_params {
 
 #define NB_FLAG_NONE            0
 #define NB_FLAG_NO_COMPENSATION 1  /* plain FP32 accumulation and update (for error studies) */
+/* Where the GPU can address pageable host memory (Grace-attached GPUs report
+ * cudaDevAttrPageableMemoryAccess), nb_write_back rewrites the caller's
+ * records directly from a kernel instead of copying to a staging buffer and
+ * scattering on the host; this flag forces the staged path (same results). */
+#define NB_FLAG_STAGED_IO 2
 
 /* FP64 diagnostics: energy, linear momentum, angular momentum (all FP64
  * reductions on the GPU). The potential is the one of the selected law:

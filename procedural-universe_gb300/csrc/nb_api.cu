@@ -113,6 +113,52 @@ __global__ void k_pack_writeback(const float4* __restrict__ pos, const float4* _
     out[i] = r;
 }
 
+// nb_write_back straight into the caller's records (host memory the GPU can
+// address).  A warp rewrites its 32 records as one contiguous run of 4-byte
+// words, so that every store is coalesced into whole cache lines over the
+// chip-to-chip link: the words of Position (0-2), Velocity (12-17) and Forces
+// (18-23) get the new values, all other words (colours, padding, mass) are
+// read back and stored unchanged.
+constexpr int kRecWords = (int)(sizeof(nb_particle) / 4);   // 26
+static_assert(sizeof(nb_particle) == 104, "reference record layout");
+
+__global__ void __launch_bounds__(256) k_writeback_records(const float4* __restrict__ pos,
+                                                           const float4* __restrict__ vel,
+                                                           const float4* __restrict__ velc,
+                                                           const float4* __restrict__ acc, int n, int zero_forces,
+                                                           uint32_t* __restrict__ out_words) {
+    const int lane = threadIdx.x & 31;
+    const long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+    if (base >= n) return;
+    const int nrec = (int)min(32LL, (long long)n - base);
+    uint32_t* w0 = out_words + base * kRecWords;
+    for (int w = lane; w < nrec * kRecWords; w += 32) {
+        const long long r = base + w / kRecWords;
+        const int o = w % kRecWords;
+        uint32_t val;
+        if (o < 3) {
+            const float4 p = pos[r];
+            val = __float_as_uint(o == 0 ? p.x : (o == 1 ? p.y : p.z));
+        } else if (o >= 12 && o < 24) {
+            const int c = ((o - 12) >> 1) % 3;
+            double d;
+            if (o < 18) {
+                const float4 v = vel[r], vc = velc[r];
+                d = c == 0 ? (double)v.x - (double)vc.x : (c == 1 ? (double)v.y - (double)vc.y : (double)v.z - (double)vc.z);
+            } else {
+                const float4 a = acc[r];
+                const double m = pos[r].w;
+                d = zero_forces ? 0.0 : m * (double)(c == 0 ? a.x : (c == 1 ? a.y : a.z));
+            }
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+            val = (o & 1) ? (uint32_t)(bits >> 32) : (uint32_t)bits;   // little-endian halves
+        } else {
+            val = w0[w];
+        }
+        w0[w] = val;
+    }
+}
+
 __global__ void k_render_fill(const float4* __restrict__ pos, const float4* __restrict__ colour, float scale, int n,
                               nb_render_vertex* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,6 +171,11 @@ __global__ void k_render_fill(const float4* __restrict__ pos, const float4* __re
     v.scale = scale;
     out[i] = v;
 }
+
+// Kernels read and write the caller's records in place: the device reports
+// that it addresses pageable host memory (Grace-attached GPUs do, over the
+// coherent chip-to-chip link) and the caller did not ask for staged copies.
+bool host_direct(const nb_sim* s) { return s->pageable_access == 1 && !(s->prm.flags & NB_FLAG_STAGED_IO); }
 
 // Device / pinned host staging of at least `bytes`, reused across calls.
 void* device_stage(nb_sim* s, size_t bytes) {
@@ -304,6 +355,10 @@ int nb_create(const nb_params* params, nb_sim** out) {
         delete s;
         return NB_ECUDA;
     }
+    if (cudaDeviceGetAttribute(&s->pageable_access, cudaDevAttrPageableMemoryAccess, s->dev) != cudaSuccess) {
+        cudaGetLastError();
+        s->pageable_access = 0;
+    }
     if (params->stream) {
         s->stream = (cudaStream_t)params->stream;
     } else {
@@ -377,7 +432,8 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
     if (!d_rec) return fail(s, NB_ENOMEM, "device staging allocation failed");
     int* d_any = (int*)((char*)d_rec + n * sizeof(nb_particle));
     cudaError_t e = cudaSuccess;
-    if (host) {
+    const nb_particle* src = d_rec;
+    if (host) {   // the copy engine moves the records faster than kernel reads of host memory
         e = cudaMemcpyAsync(d_rec, host, n * sizeof(nb_particle), cudaMemcpyHostToDevice, s->stream);
     } else {
         const nb::refseed::GalaxyFrame frame = nb::refseed::galaxy_frame(seed, n);
@@ -388,7 +444,7 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(d_any, 0, sizeof(int), s->stream);
     if (e == cudaSuccess) {
-        k_unpack_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(d_rec, (int)n, s->prm.kind, s->pos,
+        k_unpack_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(src, (int)n, s->prm.kind, s->pos,
                                                                             s->posc, s->vel, s->velc, s->finit,
                                                                             d_any, s->d_err);
         e = cudaGetLastError();
@@ -485,10 +541,18 @@ int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
     if (n == 0) return NB_OK;
     if (!particles) return fail(s, NB_EINVAL, "null particle buffer");
     cudaSetDevice(s->dev);
+    const int zero = (s->prm.kind != NB_SIM_BARNES_HUT) && !s->forces_fresh;
+    if (host_direct(s) && ((uintptr_t)particles & 3) == 0) {
+        k_writeback_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
+            s->pos, s->vel, s->velc, s->acc, (int)n, zero, reinterpret_cast<uint32_t*>(particles));
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
+        return check_device_error(s);
+    }
     WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
     WbRecord* h_wb = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
     if (!d_wb || !h_wb) return fail(s, NB_ENOMEM, "staging allocation failed");
-    const int zero = (s->prm.kind != NB_SIM_BARNES_HUT) && !s->forces_fresh;
     k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
                                                                         (int)n, zero, d_wb);
     cudaError_t e = cudaGetLastError();

@@ -117,6 +117,7 @@ struct nb_sim {
     nb_params prm{};
     int dev = 0;
     int sm_count = 0;
+    int pageable_access = 0;   // cudaDevAttrPageableMemoryAccess: kernels may address the caller's host records
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     size_t n = 0;        // bodies

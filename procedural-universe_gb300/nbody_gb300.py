@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
 NB_OK, NB_EINVAL, NB_ENOMEM, NB_ECUDA, NB_ETIMEOUT, NB_EBADSTATE, NB_ENOTSUP = 0, -1, -2, -3, -4, -5, -6
 SIM_BRUTE_FORCE, SIM_BRUTE_FORCE_GPU, SIM_BARNES_HUT = 0, 1, 2
 LAW_REFERENCE, LAW_PLUMMER = 0, 1
-FLAG_NONE, FLAG_NO_COMPENSATION = 0, 1
+FLAG_NONE, FLAG_NO_COMPENSATION, FLAG_STAGED_IO = 0, 1, 2
 
 PARTICLE_DTYPE = np.dtype(
     [
