@@ -4,10 +4,11 @@
 // Replaces Octree::CalculateForce (src/Sim/Octree.cpp:107-145) called for
 // every body by BarnesHut::Exec (src/Sim/BarnesHut.cpp:103-110).
 //
-// A warp owns 32 consecutive bodies of the key-sorted order (spatially
-// close, so their walks mostly coincide).  The warp shares one node stack in
-// shared memory; an entry is (child range of a cell, lane mask): the lanes
-// that decided to open that cell.  Popping an entry, lanes 0..7 load the
+// A warp owns 64 consecutive bodies of the key-sorted order, two per lane
+// (spatially close, so their walks mostly coincide).  The warp shares one
+// node stack in shared memory; an entry is (child range of a cell, lane mask
+// per body slot): the bodies that decided to open that cell.  Popping an
+// entry, lanes 0..7 load the
 // cell's non-empty children (one coalesced load) into a per-warp shared
 // buffer, and each lane of the mask applies the reference's per-body rule to
 // every child, so each body makes exactly the decisions of the CPU recursion:
@@ -32,6 +33,7 @@ namespace nb {
 
 constexpr int kTravBlock = 128;
 constexpr int kTravWarps = kTravBlock / 32;
+constexpr int kTravBodies = 64;   // bodies per warp: two per lane
 constexpr int kStack = 176;   // >= 7 * 21 + 8 entries: the deepest possible walk
 constexpr float kTravTiny = 1e-30f;
 constexpr unsigned kRangeBits = 28;   // stack entry: first child cell (28 bits) | child count << 28
@@ -74,7 +76,7 @@ cudaError_t tree_forces(nb_sim* sim) {
     const float S = (float)sim->prm.softening2;
     const float G = (float)sim->prm.G;
     PhaseScope ps(sim, NB_PHASE_TRAVERSE);
-    const int blocks = (n + kTravBlock - 1) / kTravBlock;
+    const int blocks = (n + kTravWarps * kTravBodies - 1) / (kTravWarps * kTravBodies);
 #define NB_TRAV(L)                                                                                          \
     k_traverse<L><<<blocks, kTravBlock, 0, st>>>(t.spos, t.vals[t.final_buf], n, t.cell_com, t.cell_meta,   \
                                                  t.cell_lo, t.n_cells, t.n_int + 1, tf, S, G, sim->acc,     \
