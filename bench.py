@@ -244,6 +244,8 @@ def run_ours(args, w):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     dt = w["dt"]
 
+    diag0 = sim.diagnostics(0.0)       # FP64 energy and angular momentum of the initial state
+
     # warm-up (untimed)
     for _ in range(args.warmup):
         sim.step(dt, 1)
@@ -290,6 +292,13 @@ def run_ours(args, w):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * n * args.steps / (total_ms * 1e-3)
+    # drift over the warm-up and timed steps (kick-drift velocities synchronised by half a kick)
+    diag1 = sim.diagnostics(0.5 * dt)
+    L0, L1 = diag0["angular_momentum"], diag1["angular_momentum"]
+    drift = {"energy_rel": (diag1["total"] - diag0["total"]) / abs(diag0["total"]),
+             "angular_momentum_rel": float(np.linalg.norm(L1 - L0) / max(np.linalg.norm(L0), 1e-300)),
+             "energy_initial": diag0["total"], "steps": args.warmup + args.steps, "dt": dt,
+             "how": "FP64 reductions on the GPU (kinetic + pairwise potential, L = sum m x × v)"}
 
     # ---- roofline of the dominant kernel ----
     # Both kernels are bounded by FP32 arithmetic issue, not by HBM: the
@@ -371,7 +380,7 @@ def run_ours(args, w):
         "gpu_launches": int(launches1.value - launches0.value),
         "clocks": clk,
         "interactions_per_step": inter_last,
-        "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)),
+        "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)), "drift": drift,
         "phases_ms_avg": {k: v_["ms_avg"] for k, v_ in phases.items()},
         "wall_s_timed_region": t_wall,
         "forms": forms,
