@@ -35,6 +35,7 @@ constexpr int kGroupMax = 64;           // bodies per traversal group (two per l
 constexpr int kGroupMinDepth = 4;       // a group cell lies >= 4 levels below its galaxy root
 constexpr int kBoxChunk = 8192;         // bodies per block of the bounding-box pass
 constexpr int kGStack = 512;            // cells waiting to be opened, per warp (<= 32 pushed per step)
+constexpr int kGMultiTop = kGStack - 155 - 32;   // stack height up to which a walk step takes several cells
 constexpr int kGCells = 64;             // accepted-cell list, per warp
 constexpr int kGBodies = 192;           // gathered leaf-bucket bodies, per warp
 constexpr int kDirTile = 128;           // sources per shared tile of the batched direct kernel
@@ -627,9 +628,13 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         if (++pops > max_pops) { bad = true; break; }
         // Take up to 8 opened cells from the top of the stack, as many as have
         // at most 32 children together; lane j tests the j-th of those children.
+        // Above kGMultiTop waiting cells a step takes one cell (a depth-first
+        // walk leaving at most 7 cells per level, 7 * 21 + 8 in all), so the
+        // stack stays below kGMultiTop + 31 + 155 < kGStack.
+        const int cap = nst <= kGMultiTop ? 8 : 1;
         int pF = 0, pn = 0;
         bool p_bad = false;
-        if (lane < 8 && lane < nst) {
+        if (lane < cap && lane < nst) {
             const int c = stk[w][nst - 1 - lane];
             const int4 pm = __ldg(&cell_meta[c]);
             pF = pm.x;
@@ -642,7 +647,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             const int t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
         }
-        const uint32_t take = __ballot_sync(0xffffffffu, lane < 8 && lane < nst && incl <= 32);
+        const uint32_t take = __ballot_sync(0xffffffffu, lane < cap && lane < nst && incl <= 32);
         const int P = __popc(take);   // >= 1: one cell has at most 8 children
         const int T = __shfl_sync(0xffffffffu, incl, P - 1);
         __syncwarp();

@@ -34,7 +34,7 @@ namespace nb {
 constexpr int kTravBlock = 128;
 constexpr int kTravWarps = kTravBlock / 32;
 constexpr int kTravBodies = 64;   // bodies per warp: two per lane
-constexpr int kStack = 176;   // >= 7 * 21 + 8 entries: the deepest possible walk
+constexpr int kStack = 384;   // stack entries per warp (a walk step pushes at most 32)
 constexpr float kTravTiny = 1e-30f;
 constexpr unsigned kRangeBits = 28;   // stack entry: first child cell (28 bits) | child count << 28
 

@@ -1,19 +1,34 @@
 // nb_traverse_kernel.cuh -- the K6 traversal kernel (included by nb_traverse.cu).
 //
-// Two bodies per lane: a warp walks for 64 consecutive bodies of the key
-// order (lane l holds bodies base + l and base + 32 + l), so each popped cell
-// and each loaded child serves twice as many bodies, and the arithmetic of
-// both bodies runs in the packed FP32x2 instructions.  Every decision is
-// still made per body exactly as the reference's recursion makes it: a stack
-// entry carries one lane mask per body slot, the distance test uses the
-// float operations of the reference (each element of a packed operation is
-// rounded like its scalar counterpart), and a body whose test does not
-// accept contributes zero through a zero mass in the packed interaction.
-// Only the rare cases take extra work: a ratio within the 2e-5 band of the
-// threshold (exactly rounded ratio) and an opened depth-cap bucket.
+// A warp walks the tree for 64 consecutive bodies of the key order, two per
+// lane (lane l holds bodies base + l and base + 32 + l).  Every body still
+// makes exactly the decisions of the reference's recursion; what changes is
+// where they are made:
+//   * Each popped cell's children are first classified for the whole group
+//     at once, one lane per child, from the group's bounding box: if even the
+//     nearest point of the box is beyond the cell's accept distance, every
+//     body of the group accepts the cell (its float r^2 exceeds the accept
+//     threshold); if even the farthest corner is inside the reject distance,
+//     every body opens it.  Both bounds carry a 1e-5 relative margin, far
+//     above the few-ulp rounding of the float distances, so a group verdict
+//     never differs from a body's own.
+//   * Cells every body accepts, and one-body leaves, go to shared-memory lists
+//     (with the lane masks of the bodies that reached them) that are evaluated
+//     densely for both bodies of every lane with the packed FP32x2
+//     instructions; cells every body opens are pushed without per-body work.
+//   * Only the remaining ("ambiguous") cells and depth-cap buckets are decided
+//     body by body, as the reference does, with the accept / reject
+//     thresholds and the exactly rounded ratio inside the 2e-5 band.
+// A stack entry carries one lane mask per body slot: the bodies that opened
+// that cell.
 #pragma once
 
 namespace nb {
+
+constexpr int kMultiTop = kStack - 176 - 32;   // stack height up to which a step takes several entries
+static_assert(kMultiTop > 0, "stack too small for multi-entry steps");
+constexpr int kListCells = 64;    // accepted cells waiting for evaluation, per warp
+constexpr int kListBodies = 64;   // one-body leaves waiting for evaluation, per warp
 
 // The interactions of a lane's two bodies with one source (its coordinates
 // broadcast in both halves); m carries the source mass per body, zero where
@@ -36,7 +51,18 @@ __device__ __forceinline__ void pair_accel_x2(float2 dx, float2 dy, float2 dz, f
     az = __ffma2_rn(w, dz, az);
 }
 
-// Pairwise force of one body q of an opened depth-cap bucket on body p.
+// A source at c acting on the lane's two bodies (negated coordinates n*).
+template <int LAW>
+__device__ __forceinline__ void source_accel_x2(const float4 c, float2 m, float2 nx, float2 ny, float2 nz, float2 S2,
+                                                float2& ax, float2& ay, float2& az) {
+    const float2 dx = __fadd2_rn(make_float2(c.x, c.x), nx);
+    const float2 dy = __fadd2_rn(make_float2(c.y, c.y), ny);
+    const float2 dz = __fadd2_rn(make_float2(c.z, c.z), nz);
+    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    pair_accel_x2<LAW>(dx, dy, dz, r2, m, S2, ax, ay, az);
+}
+
+// Pairwise force of each body of an opened depth-cap bucket on body p.
 template <int LAW>
 __device__ __forceinline__ void bucket_accel(const float4* __restrict__ spos, int first, int count, int n, int self,
                                              const float4 p, float S, float& ax, float& ay, float& az,
@@ -51,6 +77,8 @@ __device__ __forceinline__ void bucket_accel(const float4* __restrict__ spos, in
     }
 }
 
+enum : int { CL_NONE = -1, CL_SINGLE = 0, CL_ACCEPT = 1, CL_OPEN = 2, CL_DECIDE = 3, CL_EMPTY = 4 };
+
 template <int LAW>
 __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restrict__ spos,
                                                          const int32_t* __restrict__ sorder, int n,
@@ -61,49 +89,163 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                                                          float4* __restrict__ acc,
                                                          unsigned long long* __restrict__ inter,
                                                          int* __restrict__ err) {
-    __shared__ int4 stk[kTravWarps][kStack];   // (child range, lanes for body slot 0, for slot 1, 0)
-    __shared__ float4 kid_cm[kTravWarps][8];
-    __shared__ int4 kid_mt[kTravWarps][8];
+    __shared__ int4 stk[kTravWarps][kStack];   // (child range, lanes of body slot 0, of slot 1, 0)
+    __shared__ float4 kid_cm[kTravWarps][32];
+    __shared__ int4 kid_mt[kTravWarps][32];
+    __shared__ float4 lc_src[kTravWarps][kListCells];
+    __shared__ uint2 lc_mask[kTravWarps][kListCells];
+    __shared__ float4 lb_src[kTravWarps][kListBodies];
+    __shared__ int4 lb_info[kTravWarps][kListBodies];   // (body index, mask slot 0, mask slot 1, 0)
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
     const int base = (blockIdx.x * kTravWarps + w) * kTravBodies;
     const int s0 = base + lane, s1 = base + 32 + lane;
     const bool v0 = s0 < n, v1 = s1 < n;
+    if (__ballot_sync(0xffffffffu, v0) == 0u) return;   // a warp past the last body (whole warp)
     const float4 p0 = v0 ? spos[s0] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 p1 = v1 ? spos[s1] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 px = make_float2(p0.x, p1.x), py = make_float2(p0.y, p1.y), pz = make_float2(p0.z, p1.z);
     const float2 nx = make_float2(-p0.x, -p1.x), ny = make_float2(-p0.y, -p1.y), nz = make_float2(-p0.z, -p1.z);
     const float2 S2 = make_float2(S, S), z2 = make_float2(0.f, 0.f);
+    // the group's bounding box (valid bodies)
+    float glo[3], ghi[3];
+    {
+        const float a0[3] = {p0.x, p0.y, p0.z}, a1[3] = {p1.x, p1.y, p1.z};
+        for (int a = 0; a < 3; ++a) {
+            glo[a] = fminf(v0 ? a0[a] : INFINITY, v1 ? a1[a] : INFINITY);
+            ghi[a] = fmaxf(v0 ? a0[a] : -INFINITY, v1 ? a1[a] : -INFINITY);
+            for (int o = 16; o > 0; o >>= 1) {
+                glo[a] = fminf(glo[a], __shfl_xor_sync(0xffffffffu, glo[a], o));
+                ghi[a] = fmaxf(ghi[a], __shfl_xor_sync(0xffffffffu, ghi[a], o));
+            }
+        }
+    }
     float2 sx = z2, sy = z2, sz = z2, cx = z2, cy = z2, cz = z2, tx = z2, ty = z2, tz = z2;
     unsigned cnt = 0;
-    int top = 0, pops = 0;
+    int top = 0, pops = 0, ncl = 0, nbd = 0;
     bool bad = false;
 
-    // Entry being processed: children [F, F + nch) opened by the lanes of m0 / m1.
-    unsigned F = 0, nch = 1;
-    unsigned m0 = __ballot_sync(0xffffffffu, v0), m1 = __ballot_sync(0xffffffffu, v1);
+    auto fold = [&]() {
+        kahan_add(sx.x, cx.x, tx.x); kahan_add(sy.x, cy.x, ty.x); kahan_add(sz.x, cz.x, tz.x);
+        kahan_add(sx.y, cx.y, tx.y); kahan_add(sy.y, cy.y, ty.y); kahan_add(sz.y, cz.y, tz.y);
+        tx = ty = tz = z2;
+    };
+    auto flush_cells = [&]() {
+        __syncwarp();
+        for (int k = 0; k < ncl; ++k) {
+            const float4 c = lc_src[w][k];
+            const uint2 mk = lc_mask[w][k];
+            const float2 m = make_float2(((mk.x >> lane) & 1u) ? c.w : 0.f, ((mk.y >> lane) & 1u) ? c.w : 0.f);
+            source_accel_x2<LAW>(c, m, nx, ny, nz, S2, tx, ty, tz);
+        }
+        ncl = 0;
+        fold();
+        __syncwarp();
+    };
+    auto flush_bodies = [&]() {
+        __syncwarp();
+        for (int k = 0; k < nbd; ++k) {
+            const float4 b = lb_src[w][k];
+            const int4 bi = lb_info[w][k];
+            const bool i0 = (((unsigned)bi.y >> lane) & 1u) && bi.x != s0;
+            const bool i1 = (((unsigned)bi.z >> lane) & 1u) && bi.x != s1;
+            source_accel_x2<LAW>(b, make_float2(i0 ? b.w : 0.f, i1 ? b.w : 0.f), nx, ny, nz, S2, tx, ty, tz);
+        }
+        nbd = 0;
+        fold();
+        __syncwarp();
+    };
+
+    // A walk step takes up to 8 entries from the top of the stack, as many as
+    // have at most 32 children together; lane j handles the j-th of those
+    // children (cell ch), reached by the bodies of its entry's masks (cm0, cm1).
+    // The first step is the root, reached by every valid body.
+    int T = 1;
+    unsigned ch = 0;
+    unsigned cm0 = __ballot_sync(0xffffffffu, v0), cm1 = __ballot_sync(0xffffffffu, v1);
     while (true) {
-        if ((int)lane < (int)nch) {
-            kid_cm[w][lane] = __ldg(&cell_com[F + lane]);
-            kid_mt[w][lane] = __ldg(&cell_meta[F + lane]);
+        // ---- classify the children for the whole group, one lane per child ----
+        int cls = CL_NONE;
+        float4 ccm = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 cmt = make_int4(0, 0, 0, 0);
+        if ((int)lane < T) {
+            ccm = __ldg(&cell_com[ch]);
+            cmt = __ldg(&cell_meta[ch]);
+            kid_cm[w][lane] = ccm;
+            kid_mt[w][lane] = cmt;
+            const int kind = cmt.w & 15;
+            if (kind == TK_SINGLE) {
+                cls = CL_SINGLE;
+            } else if (kind != TK_INTERNAL) {
+                cls = CL_DECIDE;   // depth-cap bucket: body by body
+            } else {
+                const float c[3] = {ccm.x, ccm.y, ccm.z};
+                float dmin2 = 0.f, dmax2 = 0.f;
+                for (int a = 0; a < 3; ++a) {
+                    // nearest and farthest point of the group's box along this axis
+                    const float dn = fmaxf(0.f, fmaxf(glo[a] - c[a], c[a] - ghi[a]));
+                    const float df = fmaxf(fabsf(ghi[a] - c[a]), fabsf(glo[a] - c[a]));
+                    dmin2 = fmaf(dn, dn, dmin2);
+                    dmax2 = fmaf(df, df, dmax2);
+                }
+                const float thr_acc = __int_as_float(cmt.y), thr_rej = __int_as_float(cmt.z);
+                if (dmin2 * (1.f - 1e-5f) > thr_acc) cls = ccm.w != 0.f ? CL_ACCEPT : CL_EMPTY;
+                else if (dmax2 * (1.f + 1e-5f) < thr_rej) cls = CL_OPEN;
+                else cls = CL_DECIDE;
+            }
         }
         __syncwarp();
-        const bool a0 = (m0 >> lane) & 1u, a1 = (m1 >> lane) & 1u;
-        for (unsigned j = 0; j < nch; ++j) {
+        const unsigned bS = __ballot_sync(0xffffffffu, cls == CL_SINGLE);
+        const unsigned bA = __ballot_sync(0xffffffffu, cls == CL_ACCEPT);
+        const unsigned bO = __ballot_sync(0xffffffffu, cls == CL_OPEN);
+        const unsigned bD = __ballot_sync(0xffffffffu, cls == CL_DECIDE);
+        // one-body leaves: every body that reached them takes the pair (not the body itself)
+        if (bS) {
+            if (nbd + __popc(bS) > kListBodies) flush_bodies();
+            if (cls == CL_SINGLE) {
+                const int k = nbd + __popc(bS & lt);
+                lb_src[w][k] = ccm;
+                lb_info[w][k] = make_int4(cmt.x, (int)cm0, (int)cm1, 0);
+                unsigned c2 = __popc(cm0) + __popc(cm1);
+                const int slot = cmt.x - base;
+                if (slot >= 0 && slot < kTravBodies && (((slot < 32 ? cm0 : cm1) >> (slot & 31)) & 1u)) --c2;
+                cnt += c2;
+            }
+            nbd += __popc(bS);
+        }
+        // cells every body accepts: the monopole, for every body that reached them
+        if (bA) {
+            if (ncl + __popc(bA) > kListCells) flush_cells();
+            if (cls == CL_ACCEPT) {
+                const int k = ncl + __popc(bA & lt);
+                lc_src[w][k] = ccm;
+                lc_mask[w][k] = make_uint2(cm0, cm1);
+                cnt += __popc(cm0) + __popc(cm1);
+            }
+            ncl += __popc(bA);
+        }
+        // cells every body opens
+        if (bO) {
+            bool ok = true;
+            if (cls == CL_OPEN) {
+                const unsigned cf = (unsigned)cmt.x, cn = ((unsigned)cmt.w >> 4) & 15u;
+                ok = cf < (1u << kRangeBits) && cn >= 1 && cn <= 8 && cf + cn <= (unsigned)n_cells;
+                if (ok && top + __popc(bO) <= kStack)
+                    stk[w][top + __popc(bO & lt)] = make_int4((int)(cf | (cn << kRangeBits)), (int)cm0, (int)cm1, 0);
+            }
+            if (!__all_sync(0xffffffffu, ok) || top + __popc(bO) > kStack) bad = true;
+            top += __popc(bO);
+        }
+        // the rest: each body decides, as the reference's recursion does
+        __syncwarp();
+        for (unsigned rem = bD; rem && !bad; rem &= rem - 1u) {
+            const int j = __ffs(rem) - 1;
             const float4 cm = kid_cm[w][j];
             const int4 mt = kid_mt[w][j];
+            const unsigned pm0 = __shfl_sync(0xffffffffu, cm0, j), pm1 = __shfl_sync(0xffffffffu, cm1, j);
+            const unsigned chj = __shfl_sync(0xffffffffu, ch, j);
+            const bool a0 = (pm0 >> lane) & 1u, a1 = (pm1 >> lane) & 1u;
             const int kind = mt.w & 15;
-            if (kind == TK_SINGLE) {
-                const bool i0 = a0 && mt.x != s0, i1 = a1 && mt.x != s1;
-                if (i0 || i1) {
-                    const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
-                    const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
-                    const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
-                    const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-                    pair_accel_x2<LAW>(dx, dy, dz, r2, make_float2(i0 ? cm.w : 0.f, i1 ? cm.w : 0.f), S2, tx, ty, tz);
-                    cnt += (i0 ? 1u : 0u) + (i1 ? 1u : 0u);
-                }
-                continue;
-            }
             bool open0 = false, open1 = false;
             if (a0 || a1) {
                 // the reference's float distance: dv = p - COM, r2 = (dvx^2 + dvy^2) + dvz^2, each op rounded
@@ -113,10 +255,11 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                 const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dvx, dvx), __fmul2_rn(dvy, dvy)), __fmul2_rn(dvz, dvz));
                 const float thr_acc = __int_as_float(mt.y), thr_rej = __int_as_float(mt.z);
                 bool acc0 = r2.x > thr_acc, acc1 = r2.y > thr_acc;
-                if ((a0 && !acc0 && !(r2.x < thr_rej)) || (a1 && !acc1 && !(r2.y < thr_rej))) {
-                    const float side = __ldg(&cell_lo[F + j]).w;
-                    if (!acc0 && !(r2.x < thr_rej)) acc0 = __fdiv_rn(side, __fsqrt_rn(r2.x)) < theta_f;
-                    if (!acc1 && !(r2.y < thr_rej)) acc1 = __fdiv_rn(side, __fsqrt_rn(r2.y)) < theta_f;
+                const bool band0 = a0 && !acc0 && !(r2.x < thr_rej), band1 = a1 && !acc1 && !(r2.y < thr_rej);
+                if (band0 || band1) {
+                    const float side = __ldg(&cell_lo[chj]).w;
+                    if (band0) acc0 = __fdiv_rn(side, __fsqrt_rn(r2.x)) < theta_f;
+                    if (band1) acc1 = __fdiv_rn(side, __fsqrt_rn(r2.y)) < theta_f;
                 }
                 acc0 = acc0 && a0;
                 acc1 = acc1 && a1;
@@ -147,19 +290,50 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                 }
             }
         }
-        kahan_add(sx.x, cx.x, tx.x); kahan_add(sy.x, cy.x, ty.x); kahan_add(sz.x, cz.x, tz.x);
-        kahan_add(sx.y, cx.y, tx.y); kahan_add(sy.y, cy.y, ty.y); kahan_add(sz.y, cz.y, tz.y);
-        tx = ty = tz = z2;
-        // A well-formed tree pops each internal cell at most once per warp.
+        fold();
+        // A well-formed tree pushes each internal cell at most once per warp.
         if (bad || top == 0 || ++pops > max_pops) break;
+        // ---- next step: up to 8 entries from the top of the stack ----
+        // A step pushes at most 32 entries.  Above kMultiTop entries the walk
+        // takes one entry per step, a depth-first walk that leaves at most 7
+        // entries per tree level (7 * 21 + 8 in all), so the stack never holds
+        // more than kMultiTop + 31 + 155 < kStack entries.
         __syncwarp();
-        --top;
-        const int4 e = stk[w][top];
-        F = (unsigned)e.x & ((1u << kRangeBits) - 1u);
-        nch = (unsigned)e.x >> kRangeBits;
-        m0 = (unsigned)e.y;
-        m1 = (unsigned)e.z;
+        const int cap = top <= kMultiTop ? 8 : 1;
+        unsigned eF = 0, em0 = 0, em1 = 0;
+        int en = 0;
+        if (lane < cap && lane < top) {
+            const int4 e = stk[w][top - 1 - lane];
+            eF = (unsigned)e.x & ((1u << kRangeBits) - 1u);
+            en = (int)((unsigned)e.x >> kRangeBits);
+            em0 = (unsigned)e.y;
+            em1 = (unsigned)e.z;
+        }
+        int incl = en;   // inclusive prefix of the child counts over lanes 0..7
+        for (int o = 1; o < 8; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const unsigned take = __ballot_sync(0xffffffffu, lane < cap && lane < top && incl <= 32);
+        const int P = __popc(take);   // >= 1: an entry has at most 8 children
+        T = __shfl_sync(0xffffffffu, incl, P - 1);
         __syncwarp();
+        top -= P;
+        int q = 0;   // this lane's entry: the number of taken entries whose children end at or before it
+        for (int l = 0; l < 8; ++l) {
+            const int e = __shfl_sync(0xffffffffu, incl, l);
+            q += (l < P && e <= lane) ? 1 : 0;
+        }
+        q &= 7;
+        const unsigned qF = __shfl_sync(0xffffffffu, eF, q);
+        const int qx = __shfl_sync(0xffffffffu, incl - en, q);
+        cm0 = __shfl_sync(0xffffffffu, em0, q);
+        cm1 = __shfl_sync(0xffffffffu, em1, q);
+        ch = qF + (unsigned)(lane - qx);
+    }
+    if (!bad) {
+        flush_cells();
+        flush_bodies();
     }
     if ((bad || top > 0) && lane == 0) record_error(err, DEV_STACK_OVERFLOW);
     if (v0) acc[sorder[s0]] = make_float4(G * (sx.x - cx.x), G * (sy.x - cy.x), G * (sz.x - cz.x), 0.f);
