@@ -276,51 +276,6 @@ __global__ void k_batch_roots(const int32_t* __restrict__ slot_start, int nslot,
     root[g] = int_cell[k];
 }
 
-// ---- group traversal ----------------------------------------------------------
-template <int LAW>
-__device__ __forceinline__ void body_accel(const float4 p, const float4 b, float S, float& ax, float& ay, float& az) {
-    const float dx = b.x - p.x, dy = b.y - p.y, dz = b.z - p.z;
-    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    float w;
-    if (LAW == NB_LAW_REFERENCE) {
-        const float s = r2 + S;
-        w = b.w * rsqrt_approx(fmaf(r2 * s, s, 1e-30f));
-    } else {
-        const float inv = rsqrt_approx(r2 + S);
-        w = b.w * inv * (inv * inv);
-    }
-    ax = fmaf(w, dx, ax);
-    ay = fmaf(w, dy, ay);
-    az = fmaf(w, dz, az);
-}
-
-// Monopole with the force law plus the Newtonian quadrupole term
-// a += Q x / r^5 - 5/2 (x.Q.x) x / r^7, x = p - com.
-template <int LAW>
-__device__ __forceinline__ void cell_accel(const float4 p, const float4 cm, const float4 q1, const float4 q2, float S,
-                                           float& ax, float& ay, float& az) {
-    const float dx = cm.x - p.x, dy = cm.y - p.y, dz = cm.z - p.z;
-    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    float w;
-    if (LAW == NB_LAW_REFERENCE) {
-        const float s = r2 + S;
-        w = cm.w * rsqrt_approx(fmaf(r2 * s, s, 1e-30f));
-    } else {
-        const float inv = rsqrt_approx(r2 + S);
-        w = cm.w * inv * (inv * inv);
-    }
-    const float ir = rsqrt_approx(r2);
-    const float ir2 = ir * ir;
-    const float ir5 = ir2 * ir2 * ir;
-    const float qx = fmaf(q1.x, dx, fmaf(q2.x, dy, q2.y * dz));
-    const float qy = fmaf(q2.x, dx, fmaf(q1.y, dy, q2.z * dz));
-    const float qz = fmaf(q2.y, dx, fmaf(q2.z, dy, q1.z * dz));
-    const float c = 2.5f * fmaf(dx, qx, fmaf(dy, qy, dz * qz)) * ir5 * ir2;
-    ax += fmaf(w + c, dx, -qx * ir5);
-    ay += fmaf(w + c, dy, -qy * ir5);
-    az += fmaf(w + c, dz, -qz * ir5);
-}
-
 // ---- traversal groups from the tree --------------------------------------------
 // One thread per internal node at or below the galaxy roots.  A node that
 // cannot be a group itself emits its children that can (packing consecutive
