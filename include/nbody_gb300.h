@@ -267,6 +267,11 @@ int  nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t
 /* Uploads every galaxy, lays out the tables and sizes the tree buffers. */
 int  nb_batch_commit(nb_batch* b);
 int  nb_batch_set_tuning(nb_batch* b, const nb_tuning* t);
+/* Far field of the group traversal: an accepted cell farther from a group's
+ * centre than (group half-diagonal / eta) acts through the group's second-order
+ * local expansion instead of once per body.  Default eta = 0.02 / theta^2;
+ * 0 evaluates every accepted cell per body. */
+int  nb_batch_set_far_field(nb_batch* b, double eta);
 int  nb_batch_get_tuning(nb_batch* b, nb_tuning* t);
 /* Project autotuner: times candidate leaf sizes, then candidate direct-sum
  * tilings, for trial_steps graph replays each (state restored after each

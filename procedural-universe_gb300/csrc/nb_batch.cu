@@ -19,6 +19,11 @@ struct nb_batch {
     nb_params base{};
     size_t bh_threshold = 8192;
     double bh_theta = 0.6;
+    // far-field expansion: an accepted cell farther than (group half-diagonal / far_eta)
+    // from the group's centre acts through the group's local expansion; the
+    // expansion's relative error grows like far_eta * theta^2, hence the default
+    // far_eta = 0.02 / theta^2 (0 turns it off)
+    double far_eta = 0.0;
     nb_sim* core = nullptr;   // device state of all bodies, stream, error word, tree buffers
     std::string err;
     // galaxies as added
@@ -203,7 +208,8 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
     k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(                                                         \
         b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, t.cell_meta,      \
         b->cell_q1, b->cell_q2, b->cell_first, t.cell_count, t.cell_hi, b->gal_box, b->gal_root, b->nslot,        \
-        (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, c->acc, t.interactions, c->d_err)
+        (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, (float)(b->far_eta * b->far_eta),   \
+        100.f * S, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
             else NB_GT(NB_LAW_REFERENCE);
 #undef NB_GT
@@ -383,6 +389,7 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
     b->base = p;
     b->bh_threshold = bh_threshold;
     b->bh_theta = bh_theta;
+    b->far_eta = 0.02 / (bh_theta * bh_theta);
     b->core = core;
     if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
@@ -518,6 +525,14 @@ int nb_batch_set_tuning(nb_batch* b, const nb_tuning* t) {
     if (!b->committed) return NB_OK;
     cudaSetDevice(b->core->dev);
     return plan_units(b);
+}
+
+int nb_batch_set_far_field(nb_batch* b, double eta) {
+    if (!b) return NB_EINVAL;
+    if (!(eta >= 0.0) || eta >= 1.0) return bfail(b, NB_EINVAL, "far-field eta must be in [0, 1)");
+    b->far_eta = eta;
+    b->graph_dirty = true;
+    return NB_OK;
 }
 
 int nb_batch_get_tuning(nb_batch* b, nb_tuning* t) {

@@ -425,6 +425,79 @@ __device__ __forceinline__ void put_cell(float4 (*lst)[5], int j, float4 cm, flo
     f[16 + h] = q2.y; f[18 + h] = q2.z;
 }
 
+// Far field of a group: accepted cells that are far from the group compared
+// with its size (group half-diagonal < eta * distance from the box centre X)
+// act through a local expansion at X instead of once per body:
+//   a(X + y) = A + J y + 1/2 H(y, y),
+// A the cell's full acceleration at X (force law + quadrupole), J and H the
+// first and second derivatives of its Newtonian monopole field
+//   J_ij  = m (3 d_i d_j / r^5 - delta_ij / r^3),
+//   H_ijk = m (15 d_i d_j d_k / r^7 - 3 (delta_ik d_j + delta_jk d_i + delta_ij d_k) / r^5),
+// d = COM - X.  H is fully symmetric: xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
+constexpr int kFarTerms = 19;   // A (3), J (6: xx yy zz xy xz yz), H (10)
+struct FarField {
+    float v[kFarTerms];
+};
+
+template <int LAW>
+__device__ __forceinline__ void far_add(FarField& f, const float4 cm, const float4 q1, const float4 q2, float Xx,
+                                        float Xy, float Xz, float S) {
+    const float dx = cm.x - Xx, dy = cm.y - Xy, dz = cm.z - Xz;
+    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float m = cm.w;
+    float w;
+    if (LAW == NB_LAW_REFERENCE) {
+        const float s = r2 + S;
+        w = m * rsqrt_approx(fmaf(r2 * s, s, kTiny));
+    } else {
+        const float inv = rsqrt_approx(r2 + S);
+        w = m * inv * (inv * inv);
+    }
+    const float ir = rsqrt_approx(r2), ir2 = ir * ir, ir3 = ir2 * ir, ir5 = ir3 * ir2, ir7 = ir5 * ir2;
+    // quadrupole term at X (Q traceless: q1 = Qxx Qyy Qzz, q2 = Qxy Qxz Qyz)
+    const float qx = fmaf(q1.x, dx, fmaf(q2.x, dy, q2.y * dz));
+    const float qy = fmaf(q2.x, dx, fmaf(q1.y, dy, q2.z * dz));
+    const float qz = fmaf(q2.y, dx, fmaf(q2.z, dy, q1.z * dz));
+    const float c7 = 2.5f * fmaf(dx, qx, fmaf(dy, qy, dz * qz)) * ir7;
+    float* v = f.v;
+    v[0] += fmaf(w + c7, dx, -qx * ir5);
+    v[1] += fmaf(w + c7, dy, -qy * ir5);
+    v[2] += fmaf(w + c7, dz, -qz * ir5);
+    const float m3 = 3.f * m * ir5, m1 = m * ir3;
+    v[3] += fmaf(m3 * dx, dx, -m1);       // J xx
+    v[4] += fmaf(m3 * dy, dy, -m1);       // J yy
+    v[5] += fmaf(m3 * dz, dz, -m1);       // J zz
+    v[6] += m3 * dx * dy;                 // J xy
+    v[7] += m3 * dx * dz;                 // J xz
+    v[8] += m3 * dy * dz;                 // J yz
+    const float m15 = 15.f * m * ir7;
+    const float tx = m15 * dx, ty = m15 * dy, tz = m15 * dz;
+    v[9] += dx * fmaf(tx, dx, -3.f * m3);    // H xxx = 15 m dx^3 / r^7 - 9 m dx / r^5
+    v[10] += dy * fmaf(ty, dy, -3.f * m3);   // H yyy
+    v[11] += dz * fmaf(tz, dz, -3.f * m3);   // H zzz
+    v[12] += dy * fmaf(tx, dx, -m3);         // H xxy
+    v[13] += dz * fmaf(tx, dx, -m3);         // H xxz
+    v[14] += dx * fmaf(ty, dy, -m3);         // H xyy
+    v[15] += dz * fmaf(ty, dy, -m3);         // H yyz
+    v[16] += dx * fmaf(tz, dz, -m3);         // H xzz
+    v[17] += dy * fmaf(tz, dz, -m3);         // H yzz
+    v[18] += tx * dy * dz;                   // H xyz
+}
+
+// A + J y + 1/2 H(y, y) at offset y from the expansion centre.
+__device__ __forceinline__ void far_eval(const FarField& f, float yx, float yy, float yz, float& ax, float& ay,
+                                         float& az) {
+    const float* v = f.v;
+    const float* h = v + 9;   // xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz
+    const float xx = yx * yx, yy2 = yy * yy, zz = yz * yz, xy = yx * yy, xz = yx * yz, yz2 = yy * yz;
+    ax = v[0] + v[3] * yx + v[6] * yy + v[7] * yz +
+         0.5f * (h[0] * xx + h[5] * yy2 + h[7] * zz) + h[3] * xy + h[4] * xz + h[9] * yz2;
+    ay = v[1] + v[6] * yx + v[4] * yy + v[8] * yz +
+         0.5f * (h[3] * xx + h[1] * yy2 + h[8] * zz) + h[5] * xy + h[9] * xz + h[6] * yz2;
+    az = v[2] + v[7] * yx + v[8] * yy + v[5] * yz +
+         0.5f * (h[4] * xx + h[6] * yy2 + h[2] * zz) + h[9] * xy + h[7] * xz + h[8] * yz2;
+}
+
 // Persistent: each warp takes groups from the queue until it is empty.
 template <int LAW>
 __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
@@ -433,11 +506,13 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
     const int32_t* __restrict__ cell_first, const int32_t* __restrict__ cell_count, const float4* __restrict__ cell_hi,
     const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
-    int max_pops, int leaf_size, float theta2, float S, float G, float4* __restrict__ acc,
+    int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_min_r2,
+    float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
     __shared__ float4 lcl[kGWarps][kGCells / 2][5];
     __shared__ float4 lbd[kGWarps][kGBodies / 2][2];
+    __shared__ float ffs[kGWarps][kFarTerms][32];   // far-field partial sums, one column per lane
     __shared__ int rinc[kGWarps][32], rfst[kGWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
@@ -470,6 +545,11 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         }
     }
     const float4 gb = gal_box[grp.x];
+    // expansion centre of the group's far field and its half-diagonal squared
+    const float Xx = 0.5f * (bl[0] + bh[0]), Xy = 0.5f * (bl[1] + bh[1]), Xz = 0.5f * (bl[2] + bh[2]);
+    const float rg2 = 0.25f * ((bh[0] - bl[0]) * (bh[0] - bl[0]) + (bh[1] - bl[1]) * (bh[1] - bl[1]) +
+                               (bh[2] - bl[2]) * (bh[2] - bl[2]));
+    for (int k = 0; k < kFarTerms; ++k) ffs[w][k][lane] = 0.f;   // this lane's share of the far field
     // negated target coordinates, duplicated: the pair partner is the other list entry
     const float2 n0x = make_float2(-p0.x, -p0.x), n0y = make_float2(-p0.y, -p0.y), n0z = make_float2(-p0.z, -p0.z);
     const float2 n1x = make_float2(-p1.x, -p1.x), n1y = make_float2(-p1.y, -p1.y), n1z = make_float2(-p1.z, -p1.z);
@@ -639,6 +719,18 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             a_cell = accept && count > 2 && kind == BK_INTERNAL;
             a_range = !a_cell && (count <= leaf_size || kind != BK_INTERNAL);
             a_push = !a_cell && !a_range;
+            if (a_cell && far2 > 0.f) {
+                const float ex = ccm.x - Xx, ey = ccm.y - Xy, ez = ccm.z - Xz;
+                const float r2X = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+                if (rg2 < far2 * r2X && r2X > far_min_r2) {   // far: into the group's local expansion
+                    FarField t;
+                    for (int k = 0; k < kFarTerms; ++k) t.v[k] = 0.f;
+                    far_add<LAW>(t, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]), Xx, Xy, Xz, S);
+                    for (int k = 0; k < kFarTerms; ++k) ffs[w][k][lane] += t.v[k];
+                    cnt += (unsigned)grp.z;
+                    a_cell = false;   // accepted, not listed
+                }
+            }
             // node data outside the body range would be a corrupt tree: report, never dereference
             if (a_range && (first < 0 || count < 0 || first + count > nbodies)) a_range = false, a_bad = true;
         }
@@ -667,6 +759,20 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         flush_bodies();
     }
     fold();
+    // the group's far field: sum the lanes' partial expansions, evaluate at each body
+    if (far2 > 0.f) {
+        FarField ff;
+        for (int k = 0; k < kFarTerms; ++k) {
+            float x = ffs[w][k][lane];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            ff.v[k] = x;
+        }
+        float fx, fy, fz;
+        far_eval(ff, p0.x - Xx, p0.y - Xy, p0.z - Xz, fx, fy, fz);
+        kahan_add(s0x, c0x, fx); kahan_add(s0y, c0y, fy); kahan_add(s0z, c0z, fz);
+        far_eval(ff, p1.x - Xx, p1.y - Xy, p1.z - Xz, fx, fy, fz);
+        kahan_add(s1x, c1x, fx); kahan_add(s1y, c1y, fy); kahan_add(s1z, c1z, fz);
+    }
     if (bad && lane == 0) record_error(err, DEV_STACK_OVERFLOW);
     if (v0) acc[sorder[s0]] = make_float4(G * (s0x - c0x), G * (s0y - c0y), G * (s0z - c0z), 0.f);
     if (v1) acc[sorder[s1]] = make_float4(G * (s1x - c1x), G * (s1y - c1y), G * (s1z - c1z), 0.f);

@@ -426,6 +426,7 @@ def _bind_batch():
         "nb_batch_add": ([vp, vp, vp, sz, vp], i32),
         "nb_batch_commit": ([vp], i32),
         "nb_batch_set_tuning": ([vp, vp], i32),
+        "nb_batch_set_far_field": ([vp, f64], i32),
         "nb_batch_get_tuning": ([vp, vp], i32),
         "nb_batch_autotune": ([vp, f32, i32], i32),
         "nb_batch_step": ([vp, f32, i32], i32),
@@ -515,6 +516,9 @@ class NBodyBatch:
         for k, v in kw.items():
             setattr(t, k, v)
         self._check(lib().nb_batch_set_tuning(self._h, ctypes.byref(t)), "nb_batch_set_tuning")
+
+    def set_far_field(self, eta: float):
+        self._check(lib().nb_batch_set_far_field(self._h, eta), "nb_batch_set_far_field")
 
     def read(self, g):
         n = self.sizes[g]
