@@ -20,9 +20,10 @@ struct nb_batch {
     size_t bh_threshold = 8192;
     double bh_theta = 0.6;
     // far-field expansion: an accepted cell farther than (group half-diagonal / far_eta)
-    // from the group's centre acts through the group's local expansion; the
-    // expansion's relative error grows like far_eta * theta^2, hence the default
-    // far_eta = 0.02 / theta^2 (0 turns it off)
+    // from the group's centre acts through the group's local expansion.  The
+    // default far_eta = 0.0125 / theta^3 (0.1 at theta 0.5, 0.058 at 0.6) was
+    // calibrated on 1M-body disk galaxies to add at most ~40% to the force error
+    // of the opening rule itself (2.9e-4 -> 4.1e-4 at theta 0.5); 0 turns it off.
     double far_eta = 0.0;
     nb_sim* core = nullptr;   // device state of all bodies, stream, error word, tree buffers
     std::string err;
@@ -65,7 +66,7 @@ struct nb_batch {
     int* next_unit = nullptr;
     uint64_t direct_pairs = 0;
     // tuning and graph
-    nb_tuning tune{128, 1, 1024, 32, 128};
+    nb_tuning tune{128, 1, 1024, 16, 128};
     cudaGraphExec_t exec = nullptr;
     float graph_dt = NAN;
     bool graph_dirty = true;
@@ -389,7 +390,7 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
     b->base = p;
     b->bh_threshold = bh_threshold;
     b->bh_theta = bh_theta;
-    b->far_eta = 0.02 / (bh_theta * bh_theta);
+    b->far_eta = 0.0125 / (bh_theta * bh_theta * bh_theta);
     b->core = core;
     if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
