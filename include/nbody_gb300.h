@@ -297,9 +297,11 @@ void* nb_batch_stream(nb_batch* b);
  * bytes of the active jobs (640 bytes per body: state, sort and topology
  * scratch, tree cells with quadrupoles at twice their measured count)
  * stay within memory_budget and a slot is free, and are stepped together in
- * rounds by the batched form; a round takes at most steps_per_round steps and
- * never more than the nearest job completion, so that finished jobs leave and
- * queued ones enter between rounds.  A job keeps its state on the device for
+ * rounds by the batched form; a round takes at most steps_per_round steps,
+ * never more than the nearest job completion and, with round_seconds > 0
+ * (default 0.1), no more than fit in round_seconds at the batch's measured
+ * time per step (one step in the first round of each new batch), so that
+ * finished jobs leave and queued ones enter between rounds.  A job keeps its state on the device for
  * its whole life (moved device to device when the batch is rebuilt), so its
  * result does not depend on the jobs it shared rounds with. */
 typedef struct nb_server nb_server;
@@ -309,6 +311,9 @@ typedef struct nb_server_params {
     int      max_active;      /* slots: jobs stepped together                       */
     int      steps_per_round; /* steps per scheduling round                         */
     size_t   bh_threshold;    /* n >= this: Barnes-Hut, else direct sum             */
+    double   round_seconds;   /* a round also stops after about this much stepping
+                                 (from the measured time per step; 0: no limit), so
+                                 that arriving jobs join soon                       */
 } nb_server_params;
 typedef struct nb_job {
     uint64_t seed;

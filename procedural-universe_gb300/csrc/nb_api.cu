@@ -305,6 +305,27 @@ bool params_valid(const nb_params* p, std::string& why) {
 
 }  // namespace
 
+namespace nb {
+
+int sim_reserve_zeroed(nb_sim* s, size_t n) {
+    if (n > (size_t)INT32_MAX - kPad) return fail(s, NB_EINVAL, "too many particles");
+    cudaSetDevice(s->dev);
+    return ensure_state(s, n);
+}
+
+int sim_check_state(nb_sim* s) {
+    cudaSetDevice(s->dev);
+    if (s->n == 0) return NB_OK;
+    k_check_soa<<<(unsigned)((s->n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)s->n, s->posc, s->velc,
+                                                                      s->d_err);
+    NB_CUDA(s, cudaGetLastError());
+    const int rc = check_device_error(s);
+    if (rc) s->n = 0;
+    return rc;
+}
+
+}  // namespace nb
+
 extern "C" {
 
 int nb_default_params(nb_params* p) {

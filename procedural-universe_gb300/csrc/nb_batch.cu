@@ -53,7 +53,7 @@ struct nb_batch {
     unsigned* box_bits = nullptr;    // 6 ordered words per galaxy: min xyz, max xyz
     float4* cell_q1 = nullptr;
     float4* cell_q2 = nullptr;
-    int32_t* cell_first = nullptr;
+    int4* cell_walk = nullptr;      // per cell: (first child | first body, count, first body, kind | children << 4 | level << 8)
     size_t qcap = 0;
     // direct-sum tables
     int32_t* body_dgal = nullptr;
@@ -157,8 +157,9 @@ bool launch_direct_t(nb_batch* b, int grid, cudaStream_t st, float S) {
 }
 
 // One step (update) or one force evaluation (no update) of every galaxy,
-// enqueued on the core stream without host synchronisation.
-int enqueue_step(nb_batch* b, float dt, bool update) {
+// enqueued on the core stream without host synchronisation; tree_only stops
+// after the octree topology (enough to read its cell counts).
+int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
     nb_sim* c = b->core;
     cudaStream_t st = c->stream;
     const float S = (float)b->base.softening2;
@@ -178,20 +179,21 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
                                                                       t.keys[0], t.vals[0], t.depth);
         }
         NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth));
+        if (tree_only) return NB_OK;
         {
             PhaseScope ps(c, NB_PHASE_MASS, 3);
             NB_BCUDA(b, cudaMemsetAsync(t.int_pending, 0, t.int_cap * 4, st));
             k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
                 (int)t.int_cap, t.counters + TC_NINT, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
-                t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_first,
-                t.cell_meta, (int)t.cell_cap, n, c->d_err);
+                t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_walk,
+                t.cell_meta, t.cell_hi, (int)t.cell_cap, n, c->d_err);
             k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
                                                                  t.int_cell, t.counters + TC_NINT, (int)t.int_cap,
                                                                  b->gal_root,
                                                                  c->d_err);
             NB_BCUDA(b, cudaMemsetAsync(b->group_ctr, 0, 2 * sizeof(int), st));
             k_batch_groups<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
-                (int)t.int_cap, t.counters + TC_NINT, t.int_cell, t.cell_meta, t.cell_count, b->cell_first, t.cell_hi,
+                (int)t.int_cap, t.counters + TC_NINT, t.int_cell, b->cell_walk,
                 t.vals[0], b->body_slot, (int)t.cell_cap, n, b->groups, b->group_cap, b->group_ctr, c->d_err);
         }
         {
@@ -207,8 +209,8 @@ int enqueue_step(nb_batch* b, float dt, bool update) {
             const int blocks = std::max(1, std::min(max_blocks, c->sm_count * std::max(1, occ)));
 #define NB_GT(L)                                                                                                  \
     k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(                                                         \
-        b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, t.cell_meta,      \
-        b->cell_q1, b->cell_q2, b->cell_first, t.cell_count, t.cell_hi, b->gal_box, b->gal_root, b->nslot,        \
+        b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, b->cell_walk,     \
+        b->cell_q1, b->cell_q2, b->gal_box, b->gal_root, b->nslot,                                                \
         (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, (float)(b->far_eta * b->far_eta),   \
         100.f * S, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
@@ -249,12 +251,12 @@ int reserve_tree(nb_batch* b, size_t n_int, size_t n_cells) {
     NB_BCUDA(b, tree_reserve_graph(b->core, (int)b->n_bh, n_int, n_cells));
     const size_t cap = b->core->tree.cell_cap;
     if (cap > b->qcap) {
-        cudaFree(b->cell_q1); cudaFree(b->cell_q2); cudaFree(b->cell_first);
+        cudaFree(b->cell_q1); cudaFree(b->cell_q2); cudaFree(b->cell_walk);
         b->cell_q1 = b->cell_q2 = nullptr;
-        b->cell_first = nullptr;
+        b->cell_walk = nullptr;
         NB_BCUDA(b, cudaMalloc(&b->cell_q1, cap * sizeof(float4)));
         NB_BCUDA(b, cudaMalloc(&b->cell_q2, cap * sizeof(float4)));
-        NB_BCUDA(b, cudaMalloc(&b->cell_first, cap * sizeof(int32_t)));
+        NB_BCUDA(b, cudaMalloc(&b->cell_walk, cap * sizeof(int4)));
         b->qcap = cap;
     }
     b->graph_dirty = true;
@@ -268,7 +270,7 @@ int size_tree(nb_batch* b) {
     for (int attempt = 0; attempt < 6; ++attempt) {
         int rc = reserve_tree(b, gi, gc);
         if (rc) return rc;
-        rc = enqueue_step(b, 0.f, false);
+        rc = enqueue_step(b, 0.f, false, true);
         if (rc) return rc;
         int32_t h[TC_COUNT];
         rc = read_tree_counts(b, h);
@@ -369,6 +371,28 @@ int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const fl
 
 int batch_set_tuning_quiet(nb_batch* b, const nb_tuning& t) { return nb_batch_set_tuning(b, &t); }
 
+int batch_launch_steps(nb_batch* b, float dt, int nsteps) {
+    if (!b) return NB_EINVAL;
+    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+    if (nsteps < 0 || !std::isfinite(dt)) return bfail(b, NB_EINVAL, "bad dt or nsteps");
+    cudaSetDevice(b->core->dev);
+    if (b->graph_dirty || !(b->graph_dt == dt) || !b->exec) {
+        int rc = build_graph(b, dt);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        NB_BCUDA(b, cudaGraphLaunch(b->exec, b->core->stream));
+        b->core->prof.launches += b->graph_kernels;
+    }
+    return NB_OK;
+}
+
+int batch_wait(nb_batch* b) {
+    if (!b) return NB_EINVAL;
+    cudaSetDevice(b->core->dev);
+    return sync_check(b);
+}
+
 }  // namespace nb
 
 extern "C" {
@@ -407,7 +431,7 @@ int nb_batch_destroy(nb_batch* b) {
     if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
-                    b->box_bits, b->cell_q1, b->cell_q2, b->cell_first, b->body_dgal, b->dgal, b->units,
+                    b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
                     b->unit_comp, b->part, b->next_unit};
     for (void* p : ptrs) cudaFree(p);
     if (b->core) nb_destroy(b->core);
@@ -466,15 +490,20 @@ int nb_batch_commit(nb_batch* b) {
     b->ndgal = dgi;
     b->n_total = off;
     if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
-    std::vector<float> pos(4 * b->n_total, 0.f), vel(4 * b->n_total, 0.f);
     std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
     std::vector<int4> gal_range(b->nslot);
     b->n_real = 0;
+    // state: zeroed arrays (padding bodies are zero-mass at the origin), host
+    // galaxies copied in and validated
+    int rc = sim_reserve_zeroed(b->core, b->n_total);
+    if (rc) return bfail(b, rc, nb_last_error(b->core));
     for (size_t k = 0; k < b->gal.size(); ++k) {
         const auto& g = b->gal[k];
         if (!g.dsrc[0]) {
-            std::memcpy(&pos[4 * g.off], b->h_pos[k].data(), 16 * g.n);
-            std::memcpy(&vel[4 * g.off], b->h_vel[k].data(), 16 * g.n);
+            NB_BCUDA(b, cudaMemcpyAsync(b->core->pos + g.off, b->h_pos[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
+                                        b->core->stream));
+            NB_BCUDA(b, cudaMemcpyAsync(b->core->vel + g.off, b->h_vel[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
+                                        b->core->stream));
         }
         b->n_real += g.n;
         if (g.bh) {
@@ -485,7 +514,7 @@ int nb_batch_commit(nb_batch* b) {
             for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
         }
     }
-    int rc = nb_init_soa(b->core, pos.data(), vel.data(), b->n_total);
+    rc = sim_check_state(b->core);
     if (rc) return bfail(b, rc, nb_last_error(b->core));
     // galaxies handed over from another batch keep their exact state, compensation included
     for (const auto& g : b->gal) {
@@ -543,19 +572,8 @@ int nb_batch_get_tuning(nb_batch* b, nb_tuning* t) {
 }
 
 int nb_batch_step(nb_batch* b, float dt, int nsteps) {
-    if (!b) return NB_EINVAL;
-    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
-    if (nsteps < 0 || !std::isfinite(dt)) return bfail(b, NB_EINVAL, "bad dt or nsteps");
-    cudaSetDevice(b->core->dev);
-    if (b->graph_dirty || !(b->graph_dt == dt) || !b->exec) {
-        int rc = build_graph(b, dt);
-        if (rc) return rc;
-    }
-    for (int k = 0; k < nsteps; ++k) {
-        NB_BCUDA(b, cudaGraphLaunch(b->exec, b->core->stream));
-        b->core->prof.launches += b->graph_kernels;
-    }
-    return sync_check(b);
+    const int rc = nb::batch_launch_steps(b, dt, nsteps);
+    return rc ? rc : nb::batch_wait(b);
 }
 
 int nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4) {

@@ -12,7 +12,8 @@
 //    1/16 of the galaxy cube, consecutive small siblings packed together,
 //    oversized depth-cap buckets cut into chunks -- so a group is spatially
 //    compact and its bounding box small.  A warp takes
-//    groups from a device queue (two bodies per lane), opens a cell when the
+//    groups from a device queue (two bodies per lane; one for groups of at
+//    most 32 bodies, so that half-empty warps do no idle work), opens a cell when the
 //    cell side exceeds theta times the distance from the cell's centre of
 //    mass to the group's bounding box, and collects accepted cells (monopole
 //    + quadrupole) and leaf buckets of at most leaf_size bodies (summed body
@@ -25,6 +26,8 @@
 //    through an atomic counter, and a second kernel folds the partials.
 #pragma once
 
+#include <type_traits>
+
 namespace nb {
 
 constexpr int kSlotLevels = 7;          // 21 bits of galaxy slot
@@ -35,6 +38,7 @@ constexpr int kGroupMax = 64;           // bodies per traversal group (two per l
 constexpr int kGroupMinDepth = 4;       // a group cell lies >= 4 levels below its galaxy root
 constexpr int kBoxChunk = 8192;         // bodies per block of the bounding-box pass
 constexpr int kGStack = 512;            // cells waiting to be opened, per warp (<= 32 pushed per step)
+constexpr int kStackCellLimit = 1 << 27;   // a stack entry packs a first-child index below this with 4 bits
 constexpr int kGMultiTop = kGStack - 155 - 32;   // stack height up to which a walk step takes several cells
 constexpr int kGCells = 64;             // accepted-cell list, per warp
 constexpr int kGBodies = 192;           // gathered leaf-bucket bodies, per warp
@@ -169,10 +173,18 @@ __device__ void bucket_moments(const float4* spos, int first, int count, float4&
     q2 = make_float4(xy, xz, yz, 0.f);
 }
 
+// A cell's walk record packs what the traversal reads of it besides its centre
+// of mass: (first child or, for a leaf, first body; bodies; first body;
+// kind | children << 4 | level << 8).  A node writes its own and its leaf
+// children's.
+__device__ __forceinline__ int4 walk_record(int F, int count, int first, int kind, int nch, int level) {
+    return make_int4(F, count, first, kind | (nch << 4) | (level << 8));
+}
+
 __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* int_block, const uint32_t* int_mask,
                                const int32_t* int_first, const float4* spos, float4* cell_com, float4* cell_q1,
-                               float4* cell_q2, int32_t* cell_count, int32_t* cell_first, const int4* cell_meta,
-                               int cell_cap, int nbodies, int* err) {
+                               float4* cell_q2, int32_t* cell_count, int4* cell_walk, const int4* cell_meta,
+                               const float4* cell_hi, int cell_cap, int nbodies, int* err) {
     const int c = int_cell[k];
     const int F = 1 + int_block[k];
     const int nch = __popc(int_mask[k]);
@@ -203,6 +215,8 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
             ccm[j] = __ldcg(&cell_com[ch]);
             cq1[j] = cq2[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        if (kind != BK_INTERNAL)
+            __stcg(&cell_walk[ch], walk_record(mt.x, cnt, mt.x, kind, 0, (int)__ldcg(&cell_hi[ch]).w));
         m += ccm[j].w;
         cx = fmaf(ccm[j].w, ccm[j].x, cx); cy = fmaf(ccm[j].w, ccm[j].y, cy); cz = fmaf(ccm[j].w, ccm[j].z, cz);
         count += cnt;
@@ -224,7 +238,7 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
     __stcg(&cell_q1[c], make_float4(xx, yy, zz, 0.f));
     __stcg(&cell_q2[c], make_float4(xy, xz, yz, 0.f));
     __stcg(&cell_count[c], count);
-    __stcg(&cell_first[c], int_first[k]);
+    __stcg(&cell_walk[c], walk_record(F, count, int_first[k], BK_INTERNAL, nch, (int)__ldcg(&cell_hi[c]).w));
 }
 
 __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_dev,
@@ -234,14 +248,15 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_d
                                 const int32_t* __restrict__ int_first, const float4* __restrict__ spos,
                                 float4* __restrict__ cell_com, float4* __restrict__ cell_q1,
                                 float4* __restrict__ cell_q2, int32_t* __restrict__ cell_count,
-                                int32_t* __restrict__ cell_first, const int4* __restrict__ cell_meta, int cell_cap,
-                                int nbodies, int* __restrict__ err) {
+                                int4* __restrict__ cell_walk, const int4* __restrict__ cell_meta,
+                                const float4* __restrict__ cell_hi, int cell_cap, int nbodies,
+                                int* __restrict__ err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int ni = min(*n_int_dev, int_cap);
     if (k >= ni || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {
         finish_moments(k, int_cell, int_block, int_mask, int_first, spos, cell_com, cell_q1, cell_q2, cell_count,
-                       cell_first, cell_meta, cell_cap, nbodies, err);
+                       cell_walk, cell_meta, cell_hi, cell_cap, nbodies, err);
         if (k == 0) return;
         __threadfence();
         const int p = int_parent[k];
@@ -310,11 +325,9 @@ __device__ __forceinline__ bool groupable(int level, int count) {
 }
 
 __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_dev, const int32_t* __restrict__ int_cell,
-                               const int4* __restrict__ cell_meta, const int32_t* __restrict__ cell_count,
-                               const int32_t* __restrict__ cell_first, const float4* __restrict__ cell_hi,
-                               const int32_t* __restrict__ sorder, const int32_t* __restrict__ body_slot, int n_cells,
-                               int nbodies, int4* __restrict__ groups, int cap, int* __restrict__ n_groups,
-                               int* __restrict__ err) {
+                               const int4* __restrict__ cell_walk, const int32_t* __restrict__ sorder,
+                               const int32_t* __restrict__ body_slot, int n_cells, int nbodies,
+                               int4* __restrict__ groups, int cap, int* __restrict__ n_groups, int* __restrict__ err) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= min(*n_int_dev, int_cap)) return;
     const int c = int_cell[k];
@@ -322,12 +335,12 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
         record_error(err, DEV_TREE_OVERFLOW);
         return;
     }
-    const int level = (int)cell_hi[c].w;
-    const int cnt = cell_count[c];
+    const int4 wr = cell_walk[c];
+    const int level = wr.w >> 8;
+    const int cnt = wr.y;
     if (level < kSlotLevels) return;
     if (groupable(level, cnt)) return;   // its parent groups it
-    const int4 pm = cell_meta[c];
-    const int F = pm.x, nch = (pm.w >> 4) & 15;
+    const int F = wr.x, nch = (wr.w >> 4) & 15;
     if (F < 1 || nch > 8 || F + nch > n_cells) {
         record_error(err, DEV_TREE_OVERFLOW);
         return;
@@ -337,11 +350,11 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
     int run_first = -1, run_cnt = 0;
     for (int j = 0; j < nch; ++j) {
         const int ch = F + j;
-        const int4 mt = cell_meta[ch];
-        const int kind = mt.w & 15;
-        const int cc = cell_count[ch];
-        const int cf = kind == BK_INTERNAL ? cell_first[ch] : mt.x;
-        if (!groupable((int)cell_hi[ch].w, cc)) {
+        const int4 cw = cell_walk[ch];
+        const int kind = cw.w & 15;
+        const int cc = cw.y;
+        const int cf = cw.z;
+        if (!groupable(cw.w >> 8, cc)) {
             emit_group(run_first, run_cnt, sorder, body_slot, nbodies, groups, cap, n_groups, err);
             run_first = -1;
             run_cnt = 0;
@@ -369,7 +382,11 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_de
 // of n*) with TWO accepted cells at once (their values paired in the float2
 // operands): monopole with the force law plus the Newtonian quadrupole term,
 //   a += w x - Q x / r^5 + 5/2 (x.Q.x) x / r^7,  x = com - p,
-// w the force law's (softened) monopole factor.
+// w the force law's (softened) monopole factor.  The list holds -Q (the q*
+// arguments), which saves a negation per pair.  Under the reference law 1/r
+// comes from the law's own reciprocal square root,
+//   1/r = (r^2 + S) / sqrt(r^2 (r^2 + S)^2),
+// one multiply instead of a second reciprocal square root.
 template <int LAW>
 __device__ __forceinline__ void cell_pair_accel(float2 cx, float2 cy, float2 cz, float2 cm, float2 qxx, float2 qyy,
                                                 float2 qzz, float2 qxy, float2 qxz, float2 qyz, float2 nx, float2 ny,
@@ -380,35 +397,37 @@ __device__ __forceinline__ void cell_pair_accel(float2 cx, float2 cy, float2 cz,
     float2 r2 = __fmul2_rn(dx, dx);
     r2 = __ffma2_rn(dy, dy, r2);
     r2 = __ffma2_rn(dz, dz, r2);
-    float2 w;
+    float2 w, ir;
     if (LAW == NB_LAW_REFERENCE) {
         const float2 s = __fadd2_rn(r2, S2);
         const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, make_float2(kTiny, kTiny));
-        w = __fmul2_rn(cm, make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y)));
+        const float2 rt = make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y));
+        w = __fmul2_rn(cm, rt);
+        ir = __fmul2_rn(rt, s);
     } else {
         const float2 q = __fadd2_rn(r2, S2);
         const float2 inv = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
         w = __fmul2_rn(__fmul2_rn(cm, inv), __fmul2_rn(inv, inv));
+        ir = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
     }
-    const float2 ir = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
     const float2 ir2 = __fmul2_rn(ir, ir);
     const float2 ir5 = __fmul2_rn(__fmul2_rn(ir2, ir), ir2);
+    // q = -Q x, xqx = -x.Q.x
     const float2 qx = __ffma2_rn(qxx, dx, __ffma2_rn(qxy, dy, __fmul2_rn(qxz, dz)));
     const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
     const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
     const float2 xqx = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
-    const float2 c7 = __fmul2_rn(ir5, __fmul2_rn(ir2, make_float2(2.5f, 2.5f)));
+    const float2 c7 = __fmul2_rn(ir5, __fmul2_rn(ir2, make_float2(-2.5f, -2.5f)));
     const float2 wc = __ffma2_rn(xqx, c7, w);
-    const float2 nir5 = __fmul2_rn(ir5, make_float2(-1.f, -1.f));
-    ax = __ffma2_rn(wc, dx, __ffma2_rn(nir5, qx, ax));
-    ay = __ffma2_rn(wc, dy, __ffma2_rn(nir5, qy, ay));
-    az = __ffma2_rn(wc, dz, __ffma2_rn(nir5, qz, az));
+    ax = __ffma2_rn(wc, dx, __ffma2_rn(ir5, qx, ax));
+    ay = __ffma2_rn(wc, dy, __ffma2_rn(ir5, qy, ay));
+    az = __ffma2_rn(wc, dz, __ffma2_rn(ir5, qz, az));
 }
 
 // Shared-memory lists hold their entries in pairs, each value of the two
 // entries side by side, so that one 16-byte load yields two FP32x2 operands:
 // a body pair is (x x' y y')(z z' m m'), a cell pair (x x' y y')(z z' m m')
-// (Qxx Qxx' Qyy Qyy')(Qzz Qzz' Qxy Qxy')(Qxz Qxz' Qyz Qyz').
+// then -Q: (Qxx Qxx' Qyy Qyy')(Qzz Qzz' Qxy Qxy')(Qxz Qxz' Qyz Qyz'), negated.
 constexpr float kFarAway = 1e18f;   // position of the zero-mass cell that pads an odd list
 
 __device__ __forceinline__ void put_body(float4 (*lst)[2], int j, float4 b) {
@@ -421,8 +440,8 @@ __device__ __forceinline__ void put_cell(float4 (*lst)[5], int j, float4 cm, flo
     float* f = reinterpret_cast<float*>(lst[j >> 1]);
     const int h = j & 1;
     f[h] = cm.x; f[2 + h] = cm.y; f[4 + h] = cm.z; f[6 + h] = cm.w;
-    f[8 + h] = q1.x; f[10 + h] = q1.y; f[12 + h] = q1.z; f[14 + h] = q2.x;
-    f[16 + h] = q2.y; f[18 + h] = q2.z;
+    f[8 + h] = -q1.x; f[10 + h] = -q1.y; f[12 + h] = -q1.z; f[14 + h] = -q2.x;
+    f[16 + h] = -q2.y; f[18 + h] = -q2.z;
 }
 
 // Far field of a group: accepted cells that are far from the group compared
@@ -503,8 +522,7 @@ template <int LAW>
 __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const int4* __restrict__ groups, const int* __restrict__ n_groups_dev, int group_cap, int* __restrict__ next_group,
     const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const float4* __restrict__ cell_com,
-    const int4* __restrict__ cell_meta, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
-    const int32_t* __restrict__ cell_first, const int32_t* __restrict__ cell_count, const float4* __restrict__ cell_hi,
+    const int4* __restrict__ cell_walk, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
     const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
     int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_min_r2,
     float4* __restrict__ acc,
@@ -530,6 +548,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         continue;
     }
     const bool v0 = lane < grp.z, v1 = lane + 32 < grp.z;
+    const bool dual = grp.z > 32;   // warp-uniform: groups of at most 32 bodies evaluate one body per lane
     const int s0 = grp.y + (v0 ? lane : 0), s1 = grp.y + (v1 ? lane + 32 : 0);
     const float4 p0 = spos[s0], p1 = spos[s1];
     float bl[3], bh[3];
@@ -574,15 +593,20 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
                          make_float4(0.f, 0.f, 0.f, 0.f));
         }
         __syncwarp();
-        for (int k = 0; k < (ncl + 1) >> 1; ++k) {
-            const float4 e0 = lcl[w][k][0], e1 = lcl[w][k][1], e2 = lcl[w][k][2], e3 = lcl[w][k][3], e4 = lcl[w][k][4];
-            const float2 cx = make_float2(e0.x, e0.y), cy = make_float2(e0.z, e0.w), cz = make_float2(e1.x, e1.y);
-            const float2 cm = make_float2(e1.z, e1.w), qxx = make_float2(e2.x, e2.y), qyy = make_float2(e2.z, e2.w);
-            const float2 qzz = make_float2(e3.x, e3.y), qxy = make_float2(e3.z, e3.w), qxz = make_float2(e4.x, e4.y);
-            const float2 qyz = make_float2(e4.z, e4.w);
-            cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n0x, n0y, n0z, S2, a0x, a0y, a0z);
-            cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n1x, n1y, n1z, S2, a1x, a1y, a1z);
-        }
+        auto cell_loop = [&](auto both) {
+            for (int k = 0; k < (ncl + 1) >> 1; ++k) {
+                const float4 e0 = lcl[w][k][0], e1 = lcl[w][k][1], e2 = lcl[w][k][2], e3 = lcl[w][k][3],
+                             e4 = lcl[w][k][4];
+                const float2 cx = make_float2(e0.x, e0.y), cy = make_float2(e0.z, e0.w), cz = make_float2(e1.x, e1.y);
+                const float2 cm = make_float2(e1.z, e1.w), qxx = make_float2(e2.x, e2.y), qyy = make_float2(e2.z, e2.w);
+                const float2 qzz = make_float2(e3.x, e3.y), qxy = make_float2(e3.z, e3.w), qxz = make_float2(e4.x, e4.y);
+                const float2 qyz = make_float2(e4.z, e4.w);
+                cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+                if (decltype(both)::value)
+                    cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+            }
+        };
+        if (dual) cell_loop(std::true_type{}); else cell_loop(std::false_type{});
         cnt += nv * ncl;
         ncl = 0;
         fold();
@@ -594,25 +618,28 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         }
         __syncwarp();
         const int np = (nbd + 1) >> 1;
-        int k = 0;
+        auto body_loop = [&](auto both) {
+            int k = 0;
 #pragma unroll 1
-        for (; k + 2 <= np; k += 2) {
+            for (; k + 2 <= np; k += 2) {
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const float4 e0 = lbd[w][k + u][0], e1 = lbd[w][k + u][1];
+                for (int u = 0; u < 2; ++u) {
+                    const float4 e0 = lbd[w][k + u][0], e1 = lbd[w][k + u][1];
+                    const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
+                    const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
+                    interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+                    if (decltype(both)::value) interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+                }
+            }
+            for (; k < np; ++k) {
+                const float4 e0 = lbd[w][k][0], e1 = lbd[w][k][1];
                 const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
                 const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
                 interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
-                interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+                if (decltype(both)::value) interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
             }
-        }
-        for (; k < np; ++k) {
-            const float4 e0 = lbd[w][k][0], e1 = lbd[w][k][1];
-            const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
-            const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
-            interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
-            interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
-        }
+        };
+        if (dual) body_loop(std::true_type{}); else body_loop(std::false_type{});
         cnt += nv * nbd;
         nbd = 0;
         fold();
@@ -655,8 +682,14 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     if (root < 1 || root >= n_cells) {
         bad = true;
     } else {
-        if (lane == 0) stk[w][0] = root;
-        nst = 1;
+        const int4 rw = __ldg(&cell_walk[root]);
+        const int rF = rw.x, rn = (rw.w >> 4) & 15;
+        if ((rw.w & 15) != BK_INTERNAL || rF < 1 || rn < 1 || rn > 8 || rF + rn > n_cells || rF >= kStackCellLimit) {
+            bad = true;
+        } else {
+            if (lane == 0) stk[w][0] = (rF << 4) | rn;
+            nst = 1;
+        }
     }
     __syncwarp();
     while (nst > 0 && !bad) {
@@ -668,15 +701,11 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         // stack stays below kGMultiTop + 31 + 155 < kGStack.
         const int cap = nst <= kGMultiTop ? 8 : 1;
         int pF = 0, pn = 0;
-        bool p_bad = false;
-        if (lane < cap && lane < nst) {
-            const int c = stk[w][nst - 1 - lane];
-            const int4 pm = __ldg(&cell_meta[c]);
-            pF = pm.x;
-            pn = (pm.w >> 4) & 15;
-            if ((pm.w & 15) != BK_INTERNAL || pF < 1 || pn > 8 || pF + pn > n_cells) p_bad = true, pn = 0;
+        if (lane < cap && lane < nst) {   // a stack entry is an opened cell's (first child << 4 | children)
+            const int e = stk[w][nst - 1 - lane];
+            pF = e >> 4;
+            pn = e & 15;
         }
-        if (__any_sync(0xffffffffu, p_bad)) { bad = true; break; }
         int incl = pn;   // inclusive prefix of the child counts over lanes 0..7
         for (int o = 1; o < 8; o <<= 1) {
             const int t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -687,28 +716,28 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         const int T = __shfl_sync(0xffffffffu, incl, P - 1);
         __syncwarp();
         nst -= P;
-        int q = 0;   // source cell of this lane's child: the number of taken cells whose prefix ends at or before it
-        for (int l = 0; l < 8; ++l) {
-            const int e = __shfl_sync(0xffffffffu, incl, l);
-            q += (l < P && e <= lane) ? 1 : 0;
-        }
+        // source cell of this lane's child: the last taken cell starting at or
+        // before it (every opened cell has at least one child, so the starts differ)
+        const uint32_t starts = __reduce_or_sync(0xffffffffu, lane < P ? 1u << (incl - pn) : 0u);
+        const int q = __popc(starts & ((2u << lane) - 1u)) - 1;
         const int qF = __shfl_sync(0xffffffffu, pF, q & 7);
         const int qx = __shfl_sync(0xffffffffu, incl - pn, q & 7);
         bool a_cell = false, a_range = false, a_push = false, a_bad = false;
         float4 ccm = make_float4(0.f, 0.f, 0.f, 0.f);
-        int first = 0, count = 0, ch = 0;
+        int first = 0, count = 0, ch = 0, cF = 0, cn = 0;
         if (lane < T) {
             ch = qF + (lane - qx);
             ccm = __ldg(&cell_com[ch]);
-            const int4 mt = __ldg(&cell_meta[ch]);
-            const int kind = mt.w & 15;
-            count = __ldg(&cell_count[ch]);
-            first = kind == BK_INTERNAL ? __ldg(&cell_first[ch]) : mt.x;
+            const int4 wr = __ldg(&cell_walk[ch]);
+            const int kind = wr.w & 15;
+            count = wr.y;
+            first = wr.z;
+            cF = wr.x;
+            cn = (wr.w >> 4) & 15;
             // The group form of the reference's rule side / r < theta: r is bounded
             // below for every body of the group by the distance from the centre of
             // mass to the group's bounding box.
-            const int level = (int)__ldg(&cell_hi[ch]).w;
-            const float side = ldexpf(gb.w, kSlotLevels - level);
+            const float side = ldexpf(gb.w, kSlotLevels - (wr.w >> 8));
             float d2 = 0.f;
             const float cc[3] = {ccm.x, ccm.y, ccm.z};
             for (int a = 0; a < 3; ++a) {
@@ -733,6 +762,8 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             }
             // node data outside the body range would be a corrupt tree: report, never dereference
             if (a_range && (first < 0 || count < 0 || first + count > nbodies)) a_range = false, a_bad = true;
+            if (a_push && (cF < 1 || cn < 1 || cn > 8 || cF + cn > n_cells || cF >= kStackCellLimit))
+                a_push = false, a_bad = true;
         }
         if (__any_sync(0xffffffffu, a_bad)) { bad = true; break; }
         const uint32_t bc = __ballot_sync(0xffffffffu, a_cell);
@@ -749,7 +780,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         const uint32_t bp = __ballot_sync(0xffffffffu, a_push);
         if (bp) {
             if (nst + __popc(bp) > kGStack) { bad = true; break; }
-            if (a_push) stk[w][nst + __popc(bp & lt)] = ch;
+            if (a_push) stk[w][nst + __popc(bp & lt)] = (cF << 4) | cn;
             nst += __popc(bp);
         }
         __syncwarp();

@@ -193,11 +193,23 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D);
 cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells);
 int tree_sort_tile();
 
+// ---- state set-up without a host copy of every body (nb_api.cu) ----
+// Sizes the state arrays for n bodies, all zero (zero-mass bodies at the
+// origin), for the caller to fill by copies on sim->stream.
+int sim_reserve_zeroed(nb_sim* s, size_t n);
+// Validates positions and velocities (finite) and zeroes the compensation
+// arrays, as nb_init_soa does after its upload.
+int sim_check_state(nb_sim* s);
+
 // ---- batched form hand-over (nb_batch.cu), used by the served form ----
 int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
                      size_t n, int32_t* galaxy);
 int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,
                        const float4** velc, size_t* n);
+// nb_batch_step in two halves: enqueue the steps, then wait for them and check
+// the device's error and overflow flags.
+int batch_launch_steps(nb_batch* b, float dt, int nsteps);
+int batch_wait(nb_batch* b);
 
 // ---- profiling (nb_api.cu) ----
 // Records CUDA events around one phase on sim->stream when profiling is on

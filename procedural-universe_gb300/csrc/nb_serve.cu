@@ -8,8 +8,13 @@
 // jobs -- continuing jobs hand their state over device to device, new jobs
 // bring freshly generated initial conditions -- and the active jobs are
 // stepped together by the batched form for up to steps_per_round steps,
-// never past the nearest completion.  Every job's state stays on the device
-// from admission to completion.
+// never past the nearest completion and, when round_seconds is set, for no
+// more steps than fit in round_seconds at the batch's measured time per step
+// (the first round of a new batch takes one step to measure it), so that jobs
+// arriving meanwhile are admitted soon.  While a round runs on the device the
+// host generates the initial conditions of the queued jobs that the next
+// admission can take.  Every job's state stays on the device from admission
+// to completion.
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
 #include <chrono>
@@ -33,6 +38,7 @@ struct Job {
     nb_job spec{};
     nb_job_status st{};
     int galaxy = -1;                // index in the current batch
+    bool generated = false;         // init_pos / init_vel hold its initial conditions
     std::vector<float> init_pos, init_vel, res_pos, res_vel;
 };
 
@@ -49,6 +55,7 @@ struct nb_server {
     nb_batch* batch = nullptr;
     size_t bytes_used = 0;
     float dt = NAN;                 // dt of the active jobs
+    double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
 };
 
@@ -66,11 +73,16 @@ double now_s(const nb_server* s) {
 size_t job_bytes(const nb_job& j) { return j.n * kBytesPerBody; }
 
 int generate(Job& j) {
+    if (j.generated) return NB_OK;
     const size_t n = j.spec.n;
     j.init_pos.assign(4 * n, 0.f);
     j.init_vel.assign(4 * n, 0.f);
-    if (j.spec.model == 1) return nb_seed_plummer(j.spec.seed, n, 1.0, 1.0, j.init_pos.data(), j.init_vel.data());
-    return nb_seed_disk(j.spec.seed, n, 1.0, 1.0, 0.1, 0.1, 0.2, 0.05, j.init_pos.data(), j.init_vel.data());
+    const int rc = j.spec.model == 1
+                       ? nb_seed_plummer(j.spec.seed, n, 1.0, 1.0, j.init_pos.data(), j.init_vel.data())
+                       : nb_seed_disk(j.spec.seed, n, 1.0, 1.0, 0.1, 0.1, 0.2, 0.05, j.init_pos.data(),
+                                      j.init_vel.data());
+    j.generated = rc == NB_OK;
+    return rc;
 }
 
 // Builds a batch of the active jobs; continuing jobs take their state from
@@ -105,12 +117,14 @@ int rebuild(nb_server* s) {
     }
     if (s->batch) nb_batch_destroy(s->batch);
     s->batch = nb2;
+    s->step_s = 0;
     for (uint64_t id : s->active) {
         Job& j = s->jobs[id];
         j.init_pos.clear();
         j.init_pos.shrink_to_fit();
         j.init_vel.clear();
         j.init_vel.shrink_to_fit();
+        j.generated = false;
     }
     return NB_OK;
 }
@@ -129,6 +143,7 @@ int nb_server_default_params(nb_server_params* p) {
     p->max_active = 64;
     p->steps_per_round = 25;
     p->bh_threshold = 1024;
+    p->round_seconds = 0.1;
     return NB_OK;
 }
 
@@ -136,7 +151,7 @@ int nb_server_create(const nb_server_params* p, nb_server** out) {
     if (!p || !out) return NB_EINVAL;
     *out = nullptr;
     if (p->max_active < 1 || p->steps_per_round < 1 || p->memory_budget == 0 || p->bh_threshold < 2 ||
-        !(p->base.theta > 0))
+        !(p->base.theta > 0) || !(p->round_seconds >= 0))
         return NB_EINVAL;
     nb_server* s = new (std::nothrow) nb_server();
     if (!s) return NB_ENOMEM;
@@ -226,9 +241,34 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
     if (!s->active.empty()) {
         int k = s->prm.steps_per_round;
         for (uint64_t id : s->active) k = std::min(k, s->jobs[id].spec.steps - s->jobs[id].st.steps_done);
+        if (s->prm.round_seconds > 0) {
+            const double fit = s->step_s > 0 ? s->prm.round_seconds / s->step_s : 1.0;
+            if (fit < (double)k) k = (int)fit;
+        }
         k = std::max(k, 1);
-        int rc = nb_batch_step(s->batch, s->dt, k);
+        const double t_round = now_s(s);
+        int rc = batch_launch_steps(s->batch, s->dt, k);
         if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
+        // meanwhile: initial conditions of the queued jobs the next admission can take
+        bool generated = false;
+        {
+            int slots = s->prm.max_active - (int)s->active.size();
+            size_t bytes = s->bytes_used;
+            for (uint64_t id : s->queue) {
+                Job& j = s->jobs[id];
+                if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
+                if (j.spec.dt != s->dt) break;
+                generated |= !j.generated;
+                rc = generate(j);
+                if (rc) break;   // reported when the job is admitted
+                --slots;
+                bytes += j.st.bytes;
+            }
+        }
+        rc = batch_wait(s->batch);
+        if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
+        // a round that also generated may have outlasted its steps: keep the last clean figure
+        if (!generated || s->step_s == 0) s->step_s = (now_s(s) - t_round) / k;
         for (uint64_t id : s->active) {
             Job& j = s->jobs[id];
             j.st.steps_done += k;

@@ -10,7 +10,7 @@ import nbody_gb300 as nb
 
 class nb_server_params(ctypes.Structure):
     _fields_ = [("base", nb.nb_params), ("memory_budget", ctypes.c_size_t), ("max_active", ctypes.c_int),
-                ("steps_per_round", ctypes.c_int), ("bh_threshold", ctypes.c_size_t)]
+                ("steps_per_round", ctypes.c_int), ("bh_threshold", ctypes.c_size_t), ("round_seconds", ctypes.c_double)]
 
 
 class nb_job(ctypes.Structure):
@@ -52,7 +52,8 @@ def _bind():
 class NBodyServer:
     """Continuous-batching request loop (nb_server*)."""
 
-    def __init__(self, memory_budget=None, max_active=None, steps_per_round=None, bh_threshold=None, **base):
+    def __init__(self, memory_budget=None, max_active=None, steps_per_round=None, bh_threshold=None,
+                 round_seconds=None, **base):
         L = _bind()
         p = nb_server_params()
         L.nb_server_default_params(ctypes.byref(p))
@@ -66,6 +67,8 @@ class NBodyServer:
             p.steps_per_round = steps_per_round
         if bh_threshold is not None:
             p.bh_threshold = bh_threshold
+        if round_seconds is not None:
+            p.round_seconds = round_seconds
         self.params = p
         self._h = ctypes.c_void_p()
         rc = L.nb_server_create(ctypes.byref(p), ctypes.byref(self._h))

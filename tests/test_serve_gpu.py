@@ -75,3 +75,13 @@ def test_result_matches_batched_form():
         pb, vb = b.read(0)
     np.testing.assert_array_equal(pr, pb)
     np.testing.assert_array_equal(vr, vb)
+
+
+def test_round_length_by_time_budget():
+    """round_seconds 0: rounds of steps_per_round; a budget below one step:
+    one step per round; a large budget: one measuring step, then full rounds."""
+    for secs, rounds in ((0.0, 3), (1e-9, 10), (100.0, 4)):
+        with ns.NBodyServer(max_active=2, steps_per_round=4, bh_threshold=8192, round_seconds=secs) as s:
+            (i,), _ = run_all(s, [JOBS[0]], 10)
+            assert s.status(i)["steps_done"] == 10
+            assert s.stats()["rounds"] == rounds, (secs, s.stats())
