@@ -122,7 +122,11 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
     }
     float2 sx = z2, sy = z2, sz = z2, cx = z2, cy = z2, cz = z2, tx = z2, ty = z2, tz = z2;
     unsigned cnt = 0;
-    int top = 0, pops = 0, ncl = 0, nbd = 0;
+    // Lists fill from both ends: entries that every valid body of the warp
+    // reached (and, for a body, not one of the warp's own) from the front,
+    // evaluated without masks; the others from the back, with their masks.
+    int top = 0, pops = 0, nclf = 0, nclp = 0, nbdf = 0, nbdp = 0;
+    const unsigned vm0 = __ballot_sync(0xffffffffu, v0), vm1 = __ballot_sync(0xffffffffu, v1);
     bool bad = false;
 
     auto fold = [&]() {
@@ -132,26 +136,34 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
     };
     auto flush_cells = [&]() {
         __syncwarp();
-        for (int k = 0; k < ncl; ++k) {
+        for (int k = 0; k < nclf; ++k) {
+            const float4 c = lc_src[w][k];
+            source_accel_x2<LAW>(c, make_float2(c.w, c.w), nx, ny, nz, S2, tx, ty, tz);
+        }
+        for (int k = kListCells - nclp; k < kListCells; ++k) {
             const float4 c = lc_src[w][k];
             const uint2 mk = lc_mask[w][k];
             const float2 m = make_float2(((mk.x >> lane) & 1u) ? c.w : 0.f, ((mk.y >> lane) & 1u) ? c.w : 0.f);
             source_accel_x2<LAW>(c, m, nx, ny, nz, S2, tx, ty, tz);
         }
-        ncl = 0;
+        nclf = nclp = 0;
         fold();
         __syncwarp();
     };
     auto flush_bodies = [&]() {
         __syncwarp();
-        for (int k = 0; k < nbd; ++k) {
+        for (int k = 0; k < nbdf; ++k) {
+            const float4 b = lb_src[w][k];
+            source_accel_x2<LAW>(b, make_float2(b.w, b.w), nx, ny, nz, S2, tx, ty, tz);
+        }
+        for (int k = kListBodies - nbdp; k < kListBodies; ++k) {
             const float4 b = lb_src[w][k];
             const int4 bi = lb_info[w][k];
             const bool i0 = (((unsigned)bi.y >> lane) & 1u) && bi.x != s0;
             const bool i1 = (((unsigned)bi.z >> lane) & 1u) && bi.x != s1;
             source_accel_x2<LAW>(b, make_float2(i0 ? b.w : 0.f, i1 ? b.w : 0.f), nx, ny, nz, S2, tx, ty, tz);
         }
-        nbd = 0;
+        nbdf = nbdp = 0;
         fold();
         __syncwarp();
     };
@@ -200,29 +212,43 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
         const unsigned bO = __ballot_sync(0xffffffffu, cls == CL_OPEN);
         const unsigned bD = __ballot_sync(0xffffffffu, cls == CL_DECIDE);
         // one-body leaves: every body that reached them takes the pair (not the body itself)
+        const bool reach_all = cm0 == vm0 && cm1 == vm1;
         if (bS) {
-            if (nbd + __popc(bS) > kListBodies) flush_bodies();
+            if (nbdf + nbdp + __popc(bS) > kListBodies) flush_bodies();
+            const int slot = cmt.x - base;
+            const bool own = slot >= 0 && slot < kTravBodies;
+            const unsigned bSf = __ballot_sync(0xffffffffu, cls == CL_SINGLE && reach_all && !own);
             if (cls == CL_SINGLE) {
-                const int k = nbd + __popc(bS & lt);
-                lb_src[w][k] = ccm;
-                lb_info[w][k] = make_int4(cmt.x, (int)cm0, (int)cm1, 0);
+                if ((bSf >> lane) & 1u) {
+                    lb_src[w][nbdf + __popc(bSf & lt)] = ccm;
+                } else {
+                    const int k = kListBodies - 1 - (nbdp + __popc(bS & ~bSf & lt));
+                    lb_src[w][k] = ccm;
+                    lb_info[w][k] = make_int4(cmt.x, (int)cm0, (int)cm1, 0);
+                }
                 unsigned c2 = __popc(cm0) + __popc(cm1);
-                const int slot = cmt.x - base;
-                if (slot >= 0 && slot < kTravBodies && (((slot < 32 ? cm0 : cm1) >> (slot & 31)) & 1u)) --c2;
+                if (own && (((slot < 32 ? cm0 : cm1) >> (slot & 31)) & 1u)) --c2;
                 cnt += c2;
             }
-            nbd += __popc(bS);
+            nbdf += __popc(bSf);
+            nbdp += __popc(bS & ~bSf);
         }
         // cells every body accepts: the monopole, for every body that reached them
         if (bA) {
-            if (ncl + __popc(bA) > kListCells) flush_cells();
+            if (nclf + nclp + __popc(bA) > kListCells) flush_cells();
+            const unsigned bAf = __ballot_sync(0xffffffffu, cls == CL_ACCEPT && reach_all);
             if (cls == CL_ACCEPT) {
-                const int k = ncl + __popc(bA & lt);
-                lc_src[w][k] = ccm;
-                lc_mask[w][k] = make_uint2(cm0, cm1);
+                if ((bAf >> lane) & 1u) {
+                    lc_src[w][nclf + __popc(bAf & lt)] = ccm;
+                } else {
+                    const int k = kListCells - 1 - (nclp + __popc(bA & ~bAf & lt));
+                    lc_src[w][k] = ccm;
+                    lc_mask[w][k] = make_uint2(cm0, cm1);
+                }
                 cnt += __popc(cm0) + __popc(cm1);
             }
-            ncl += __popc(bA);
+            nclf += __popc(bAf);
+            nclp += __popc(bA & ~bAf);
         }
         // cells every body opens
         if (bO) {
@@ -319,12 +345,10 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
         T = __shfl_sync(0xffffffffu, incl, P - 1);
         __syncwarp();
         top -= P;
-        int q = 0;   // this lane's entry: the number of taken entries whose children end at or before it
-        for (int l = 0; l < 8; ++l) {
-            const int e = __shfl_sync(0xffffffffu, incl, l);
-            q += (l < P && e <= lane) ? 1 : 0;
-        }
-        q &= 7;
+        // this lane's entry: the last taken entry whose children start at or
+        // before it (every entry has at least one child, so the starts differ)
+        const unsigned starts = __reduce_or_sync(0xffffffffu, lane < P ? 1u << (incl - en) : 0u);
+        const int q = (__popc(starts & ((2u << lane) - 1u)) - 1) & 7;
         const unsigned qF = __shfl_sync(0xffffffffu, eF, q);
         const int qx = __shfl_sync(0xffffffffu, incl - en, q);
         cm0 = __shfl_sync(0xffffffffu, em0, q);
