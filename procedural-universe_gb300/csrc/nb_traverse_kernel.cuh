@@ -104,7 +104,6 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
     if (__ballot_sync(0xffffffffu, v0) == 0u) return;   // a warp past the last body (whole warp)
     const float4 p0 = v0 ? spos[s0] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 p1 = v1 ? spos[s1] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2 px = make_float2(p0.x, p1.x), py = make_float2(p0.y, p1.y), pz = make_float2(p0.z, p1.z);
     const float2 nx = make_float2(-p0.x, -p1.x), ny = make_float2(-p0.y, -p1.y), nz = make_float2(-p0.z, -p1.z);
     const float2 S2 = make_float2(S, S), z2 = make_float2(0.f, 0.f);
     // the group's bounding box (valid bodies)
@@ -274,11 +273,12 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
             const int kind = mt.w & 15;
             bool open0 = false, open1 = false;
             if (a0 || a1) {
-                // the reference's float distance: dv = p - COM, r2 = (dvx^2 + dvy^2) + dvz^2, each op rounded
-                const float2 dvx = __fadd2_rn(px, make_float2(-cm.x, -cm.x));
-                const float2 dvy = __fadd2_rn(py, make_float2(-cm.y, -cm.y));
-                const float2 dvz = __fadd2_rn(pz, make_float2(-cm.z, -cm.z));
-                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dvx, dvx), __fmul2_rn(dvy, dvy)), __fmul2_rn(dvz, dvz));
+                // the reference's float distance: dv = p - COM, r2 = (dvx^2 + dvy^2) + dvz^2, each op
+                // rounded; d = COM - p = -dv exactly (rounding is symmetric), so r2 is the same
+                const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+                const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+                const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
                 const float thr_acc = __int_as_float(mt.y), thr_rej = __int_as_float(mt.z);
                 bool acc0 = r2.x > thr_acc, acc1 = r2.y > thr_acc;
                 const bool band0 = a0 && !acc0 && !(r2.x < thr_rej), band1 = a1 && !acc1 && !(r2.y < thr_rej);
@@ -290,9 +290,8 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                 acc0 = acc0 && a0;
                 acc1 = acc1 && a1;
                 if ((acc0 || acc1) && cm.w != 0.f) {
-                    pair_accel_x2<LAW>(make_float2(-dvx.x, -dvx.y), make_float2(-dvy.x, -dvy.y),
-                                       make_float2(-dvz.x, -dvz.y), r2,
-                                       make_float2(acc0 ? cm.w : 0.f, acc1 ? cm.w : 0.f), S2, tx, ty, tz);
+                    pair_accel_x2<LAW>(dx, dy, dz, r2, make_float2(acc0 ? cm.w : 0.f, acc1 ? cm.w : 0.f), S2, tx, ty,
+                                       tz);
                     cnt += (acc0 ? 1u : 0u) + (acc1 ? 1u : 0u);
                 }
                 if (kind == TK_INTERNAL) {
