@@ -17,8 +17,9 @@ Workloads (seeded synthetic galaxies; no dataset is involved):
   direct4096  direct sum, N=4096 Plummer sphere, eps=0.01, dt=1e-3
 
   batch512    512 galaxies, n log-uniform in [256, 65,536] (batched form)
-  served      Poisson stream of galaxy jobs, n log-uniform in [1,024, 1,048,576]
-              (served form: continuous batching under a memory budget)
+  served      Poisson stream of 200 galaxy jobs (200 per second; --requests),
+              n log-uniform in [1,024, 1,048,576] (served form: continuous
+              batching under a memory budget)
   bh1m_batched  the batched form (group traversal, quadrupoles) on the bh1m galaxy
 
 The default line (bh1m, one GPU) also carries "forms": the batched and the
@@ -432,6 +433,8 @@ def main():
     ap.add_argument("--workload", default="bh1m", choices=sorted(WORKLOADS) + ["batch512", "served", "bh1m_batched"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=200,
+                    help="jobs in the served workload's Poisson stream (--workload served)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched and served forms reported beside the plain-path line")
     args = ap.parse_args()

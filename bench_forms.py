@@ -10,8 +10,8 @@ reference's per-body Barnes-Hut at the same theta, or direct sum) on the
 same GPU, and with the CPU restatement of the reference on a 16-galaxy
 sample.
 
-served: Poisson arrivals (seeded) of galaxy-generation jobs, n log-uniform in
-[1,024, 1,048,576], disk + bulge as in the 1M-body workload, 200 steps each,
+served: Poisson arrivals (seeded, 200 per second) of 200 galaxy-generation jobs,
+n log-uniform in [1,024, 1,048,576], disk + bulge as in the 1M-body workload, 200 steps each,
 Barnes-Hut theta=0.5, admitted against a 120 GB device-memory budget and
 stepped together by continuous batching (see nb_server_* in the C-ABI).
 """
@@ -23,6 +23,7 @@ import time
 import numpy as np
 
 METRIC = "body-steps/s"
+SERVED_REQUESTS = 200   # jobs in the served stream (mean n about 154,000, arrivals over about 1 s)
 
 
 def batch_galaxies(nb, seed=2024, count=512, lo=256, hi=65536):
@@ -111,7 +112,7 @@ def cpu_sample(gals, eps2, theta, threshold, count=16, seed=7, budget_s=20.0):
                       "for n >= %d, direct sum below) on all host cores" % (len(done), n_tot, theta, threshold)}
 
 
-def served_stream(requests=48, rate=200.0):
+def served_stream(requests=SERVED_REQUESTS, rate=200.0):
     """Seeded Poisson arrivals and log-uniform job sizes in [1,024, 1,048,576]."""
     rng = np.random.default_rng(5)
     gaps = rng.exponential(1.0 / rate, requests)
@@ -128,7 +129,7 @@ def reference_line(args, nb, workload):
         cpu = cpu_sample(gals, 1e-4, 0.6, 8192)
         cfg = {"workload": "batch512", "galaxies": len(gals)}
     else:
-        _, sizes = served_stream()
+        _, sizes = served_stream(getattr(args, "requests", SERVED_REQUESTS))
         gals = [nb.seed_disk(10_000 + k, int(n)) for k, n in enumerate(sizes)]
         cpu = cpu_sample(gals, 0.005 ** 2, 0.5, 1024, count=len(gals))
         cfg = {"workload": "served", "requests": len(sizes)}
@@ -139,8 +140,10 @@ def reference_line(args, nb, workload):
             "e2e": {"value": cpu["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def run_served(args, nb, torch, requests=48, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
+def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
     import nbody_serve as ns
+    if requests is None:
+        requests = getattr(args, "requests", SERVED_REQUESTS)
     arrivals, sizes = served_stream(requests, rate)
     # warm-up: one small Barnes-Hut job and one direct-sum job through a server of
     # the same settings, so that first-use module loading is not in the stream
