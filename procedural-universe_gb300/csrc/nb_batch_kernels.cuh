@@ -7,20 +7,21 @@
 //    levels), so ONE radix sort and ONE topology build make a forest whose
 //    level-7 nodes are the galaxy roots.
 //  * The mass pass adds traceless quadrupole moments (parallel-axis rule
-//    bottom-up).  Traversal groups are taken from the tree itself: the
-//    largest subtrees of at most kGroupMax bodies whose cell is at most
-//    1/16 of the galaxy cube, consecutive small siblings packed together,
-//    oversized depth-cap buckets cut into chunks -- so a group is spatially
-//    compact and its bounding box small.  A warp takes
-//    groups from a device queue (two bodies per lane; one for groups of at
-//    most 32 bodies, so that half-empty warps do no idle work), opens a cell when the
-//    cell side exceeds theta times the distance from the cell's centre of
-//    mass to the group's bounding box, and collects accepted cells (monopole
-//    + quadrupole) and leaf buckets of at most leaf_size bodies (summed body
-//    by body) in shared-memory lists that every lane then evaluates for both
-//    of its bodies with the packed FP32x2 instructions.  This is a
-//    performance form whose parity is the force error against the FP64
-//    direct sum (<= 1e-3), not the reference's per-body opening rule.
+//    bottom-up) and a 16-byte walk record per cell.  Traversal groups are
+//    taken from the tree itself: the largest subtrees of at most kGroupMax
+//    bodies whose cell is at most 1/16 of the galaxy cube, consecutive small
+//    siblings packed together, oversized depth-cap buckets cut into chunks --
+//    so a group is spatially compact and its bounding box small.  A warp
+//    takes groups from a device queue (two bodies per lane; one for groups of
+//    at most 32 bodies, so that half-empty warps do no idle work), opens a
+//    cell when the cell side exceeds theta times the distance from the cell's
+//    centre of mass to the group's bounding box, and collects accepted cells
+//    (monopole + quadrupole) and leaf buckets of at most leaf_size bodies
+//    (summed body by body) in shared-memory lists that every lane then
+//    evaluates for its bodies with the packed FP32x2 instructions; accepted
+//    cells far from the group go into the group's local expansion instead.
+//    This is a performance form whose parity is the force error against the
+//    FP64 direct sum (<= 1e-3), not the reference's per-body opening rule.
 //  * Direct-sum members are padded to multiples of 256 bodies; a persistent
 //    kernel takes (galaxy, target block, source range) units from a table
 //    through an atomic counter, and a second kernel folds the partials.
