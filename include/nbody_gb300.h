@@ -269,7 +269,7 @@ int  nb_batch_commit(nb_batch* b);
 int  nb_batch_set_tuning(nb_batch* b, const nb_tuning* t);
 /* Far field of the group traversal: an accepted cell farther from a group's
  * centre than (group half-diagonal / eta) acts through the group's second-order
- * local expansion instead of once per body.  Default eta = 0.0125 / theta^3;
+ * local expansion instead of once per body.  Default eta = 0.025 / theta^3;
  * 0 evaluates every accepted cell per body. */
 int  nb_batch_set_far_field(nb_batch* b, double eta);
 int  nb_batch_get_tuning(nb_batch* b, nb_tuning* t);

@@ -21,9 +21,10 @@ struct nb_batch {
     double bh_theta = 0.6;
     // far-field expansion: an accepted cell farther than (group half-diagonal / far_eta)
     // from the group's centre acts through the group's local expansion.  The
-    // default far_eta = 0.0125 / theta^3 (0.1 at theta 0.5, 0.058 at 0.6) was
-    // calibrated on 1M-body disk galaxies to add at most ~40% to the force error
-    // of the opening rule itself (2.9e-4 -> 4.1e-4 at theta 0.5); 0 turns it off.
+    // default far_eta = 0.025 / theta^3 (0.2 at theta 0.5, 0.116 at 0.6) was
+    // calibrated on disk galaxies of 10^4 to 10^6 bodies to add at most ~35% to
+    // the force error of the opening rule itself (2.9e-4 -> 3.8e-4 on the 1M-body
+    // galaxy at theta 0.5); 0 turns it off.
     double far_eta = 0.0;
     nb_sim* core = nullptr;   // device state of all bodies, stream, error word, tree buffers
     std::string err;
@@ -414,7 +415,7 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
     b->base = p;
     b->bh_threshold = bh_threshold;
     b->bh_theta = bh_theta;
-    b->far_eta = 0.0125 / (bh_theta * bh_theta * bh_theta);
+    b->far_eta = 0.025 / (bh_theta * bh_theta * bh_theta);
     b->core = core;
     if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();

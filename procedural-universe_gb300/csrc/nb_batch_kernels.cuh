@@ -449,11 +449,15 @@ __device__ __forceinline__ void put_cell(float4 (*lst)[5], int j, float4 cm, flo
 // with its size (group half-diagonal < eta * distance from the box centre X)
 // act through a local expansion at X instead of once per body:
 //   a(X + y) = A + J y + 1/2 H(y, y),
-// A the cell's full acceleration at X (force law + quadrupole), J and H the
-// first and second derivatives of its Newtonian monopole field
-//   J_ij  = m (3 d_i d_j / r^5 - delta_ij / r^3),
+// A the cell's full acceleration at X (force law + quadrupole), J the first
+// derivative of its Newtonian monopole + quadrupole field and H the second
+// derivative of the monopole field:
+//   J_ij  = m (3 d_i d_j / r^5 - delta_ij / r^3)
+//         + Q_ij / r^5 - 5 ((Qd)_i d_j + (Qd)_j d_i) / r^7 - 5/2 s delta_ij / r^7 + 35/2 s d_i d_j / r^9,
 //   H_ijk = m (15 d_i d_j d_k / r^7 - 3 (delta_ik d_j + delta_jk d_i + delta_ij d_k) / r^5),
-// d = COM - X.  H is fully symmetric: xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
+// d = COM - X, s = d.Q.d (the quadrupole part of J is minus the derivative,
+// with respect to d, of the quadrupole acceleration -Q d / r^5 + 5/2 s d / r^7).
+// H is fully symmetric: xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
 constexpr int kFarTerms = 19;   // A (3), J (6: xx yy zz xy xz yz), H (10)
 struct FarField {
     float v[kFarTerms];
@@ -478,18 +482,20 @@ __device__ __forceinline__ void far_add(FarField& f, const float4 cm, const floa
     const float qx = fmaf(q1.x, dx, fmaf(q2.x, dy, q2.y * dz));
     const float qy = fmaf(q2.x, dx, fmaf(q1.y, dy, q2.z * dz));
     const float qz = fmaf(q2.y, dx, fmaf(q2.z, dy, q1.z * dz));
-    const float c7 = 2.5f * fmaf(dx, qx, fmaf(dy, qy, dz * qz)) * ir7;
+    const float sq = fmaf(dx, qx, fmaf(dy, qy, dz * qz));   // d.Q.d
+    const float c7 = 2.5f * sq * ir7;
     float* v = f.v;
     v[0] += fmaf(w + c7, dx, -qx * ir5);
     v[1] += fmaf(w + c7, dy, -qy * ir5);
     v[2] += fmaf(w + c7, dz, -qz * ir5);
     const float m3 = 3.f * m * ir5, m1 = m * ir3;
-    v[3] += fmaf(m3 * dx, dx, -m1);       // J xx
-    v[4] += fmaf(m3 * dy, dy, -m1);       // J yy
-    v[5] += fmaf(m3 * dz, dz, -m1);       // J zz
-    v[6] += m3 * dx * dy;                 // J xy
-    v[7] += m3 * dx * dz;                 // J xz
-    v[8] += m3 * dy * dz;                 // J yz
+    const float t5 = 5.f * ir7, g9 = 17.5f * sq * ir7 * ir2, dg = m1 + c7;   // c7 = 5/2 s / r^7
+    v[3] += fmaf(m3 * dx, dx, -dg) + fmaf(q1.x, ir5, dx * fmaf(g9, dx, -2.f * t5 * qx));   // J xx
+    v[4] += fmaf(m3 * dy, dy, -dg) + fmaf(q1.y, ir5, dy * fmaf(g9, dy, -2.f * t5 * qy));   // J yy
+    v[5] += fmaf(m3 * dz, dz, -dg) + fmaf(q1.z, ir5, dz * fmaf(g9, dz, -2.f * t5 * qz));   // J zz
+    v[6] += fmaf(m3 * dx + g9 * dx, dy, fmaf(q2.x, ir5, -t5 * fmaf(qx, dy, qy * dx)));     // J xy
+    v[7] += fmaf(m3 * dx + g9 * dx, dz, fmaf(q2.y, ir5, -t5 * fmaf(qx, dz, qz * dx)));     // J xz
+    v[8] += fmaf(m3 * dy + g9 * dy, dz, fmaf(q2.z, ir5, -t5 * fmaf(qy, dz, qz * dy)));     // J yz
     const float m15 = 15.f * m * ir7;
     const float tx = m15 * dx, ty = m15 * dy, tz = m15 * dz;
     v[9] += dx * fmaf(tx, dx, -3.f * m3);    // H xxx = 15 m dx^3 / r^7 - 9 m dx / r^5
