@@ -84,6 +84,28 @@ def dist_env():
     return world, rank, local
 
 
+# ---- replicas: one independent galaxy per rank, no data-path collective ----
+def replica_seed(rank: int) -> int:
+    """Seed of rank's galaxy: every replica steps a different galaxy."""
+    return 1234 + rank
+
+
+def max_over_ranks(x: float, device="cpu") -> float:
+    """The largest x over the ranks of the process group (x itself without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(world: int, n: int, steps: int, max_total_ms: float) -> float:
+    """Body-steps/s of all replicas together, timed by the slowest rank."""
+    return world * n * steps / (max_total_ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -235,7 +257,7 @@ def run_ours(args, w):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     n = w["n"]
-    pm, v = seed_workload(w, 1234 + rank)
+    pm, v = seed_workload(w, replica_seed(rank))
     stream = torch.cuda.Stream(device=dev)
     sim = nb.NBodySim(kind=w["kind"], device=dev, softening2=w["eps"] ** 2, theta=w["theta"],
                       stream=stream.cuda_stream)
@@ -288,11 +310,8 @@ def run_ours(args, w):
         if cnt.value:
             phases[nm] = {"ms_total": ms.value, "launches": int(cnt.value), "ms_avg": ms.value / cnt.value}
     lib.nb_profile_enable(sim.handle, 0)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * args.steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(total_ms, device="cuda")
+    value = replicas_value(world, n, args.steps, total_ms)
     # drift over the warm-up and timed steps (kick-drift velocities synchronised by half a kick)
     diag1 = sim.diagnostics(0.5 * dt)
     L0, L1 = diag0["angular_momentum"], diag1["angular_momentum"]
@@ -350,9 +369,10 @@ def run_ours(args, w):
             sim.step(dt, 1)
             sim.write_back(host)      # D2H of the result into the records
         torch.cuda.synchronize()
-        t_e2e = time.perf_counter() - t0
-        e2e = {"value": world * n * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": n * 104,
-               "d2h_bytes_per_step": n * 64, "steps": e2e_steps}
+        t_e2e = max_over_ranks(time.perf_counter() - t0, device="cuda")
+        e2e = {"value": replicas_value(world, n, e2e_steps, t_e2e * 1e3), "unit": METRIC,
+               "h2d_bytes_per_step": n * 104,
+               "d2h_bytes_per_step": n * (104 if sim.write_back_direct() else 64), "steps": e2e_steps}
 
     # ---- force error vs the FP64 oracle on the GPU (sampled targets) ----
     rng = np.random.default_rng(1)

@@ -158,6 +158,11 @@ int  nb_synchronize(nb_sim* sim);
  * (src/Sim/BruteForceCPU.cpp:72) and hold the last Barnes-Hut force otherwise
  * (src/Sim/BarnesHut.cpp:81-95). Colour, OriginalColour and Mass are untouched. */
 int  nb_write_back(nb_sim* sim, nb_particle* particles, size_t n);
+/* 1 when nb_write_back rewrites the caller's records from the GPU directly
+ * (whole 104-byte records, see NB_FLAG_STAGED_IO), 0 when it copies 64-byte
+ * packed records to a staging buffer and scatters them on the host; -1 for
+ * a null handle. */
+int  nb_write_back_direct(const nb_sim* sim);
 
 /* Host copies of the state. Any pointer may be NULL. force3 is the force
  * (m * acceleration) of the last force evaluation. */

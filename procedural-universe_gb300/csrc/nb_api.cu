@@ -556,6 +556,8 @@ int nb_read_state(nb_sim* s, float* pos3, double* vel3, double* force3) {
     return NB_OK;
 }
 
+int nb_write_back_direct(const nb_sim* s) { return s ? (host_direct(s) ? 1 : 0) : -1; }
+
 int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
     if (!s) return NB_EINVAL;
     if (n != s->n) return fail(s, NB_EINVAL, "record count differs from the initialised count");

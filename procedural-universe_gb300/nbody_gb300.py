@@ -116,6 +116,7 @@ def lib() -> ctypes.CDLL:
             "nb_step": ([vp, f32, i32], i32),
             "nb_synchronize": ([vp], i32),
             "nb_write_back": ([vp, vp, sz], i32),
+            "nb_write_back_direct": ([vp], i32),
             "nb_read_state": ([vp, vp, vp, vp], i32),
             "nb_compute_forces": ([vp, vp], i32),
             "nb_last_interactions": ([vp, vp], i32),
@@ -323,6 +324,10 @@ class NBodySim:
     def write_back(self, particles: np.ndarray):
         assert particles.dtype == PARTICLE_DTYPE and particles.flags.c_contiguous
         self._check(lib().nb_write_back(self._h, _ptr(particles), particles.shape[0]), "nb_write_back")
+
+    def write_back_direct(self) -> bool:
+        """Whether write_back rewrites the records from the GPU directly (whole records)."""
+        return lib().nb_write_back_direct(self._h) == 1
 
     def read_state(self):
         pos = np.zeros((self.n, 3), np.float32)
