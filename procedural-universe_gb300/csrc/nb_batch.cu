@@ -277,6 +277,10 @@ int size_tree(nb_batch* b) {
         rc = read_tree_counts(b, h);
         if (rc) return rc;
         const size_t ni = (size_t)h[TC_NINT], nc = (size_t)h[TC_NINT] + (size_t)h[TC_NLEAF];
+        // the traversal's stack entries carry a cell index below kStackCellLimit
+        if (nc >= (size_t)kStackCellLimit)
+            return bfail(b, NB_EINVAL, "batch too large: its octree needs more than 2^27 cells (about 10^8 "
+                                       "Barnes-Hut bodies); split it over several batches");
         if (h[TC_OVERFLOW] == 0 && ni <= b->core->tree.int_cap && nc <= b->core->tree.cell_cap) {
             // room for the tree to grow as the galaxies evolve
             return reserve_tree(b, 2 * ni + 64, 2 * nc + 64);
