@@ -301,7 +301,8 @@ void* nb_batch_stream(nb_batch* b);
 /* Jobs arrive, wait in a FIFO queue, are admitted while the estimated device
  * bytes of the active jobs (640 bytes per body: state, sort and topology
  * scratch, tree cells with quadrupoles at twice their measured count)
- * stay within memory_budget and a slot is free, and are stepped together in
+ * stay within memory_budget, their bodies within 96 Mi (the batched octree's
+ * cell-index range; a larger job is rejected) and a slot is free, and are stepped together in
  * rounds by the batched form; a round takes at most steps_per_round steps,
  * never more than the nearest job completion and, with round_seconds > 0
  * (default 0.1), no more than fit in round_seconds at the batch's measured

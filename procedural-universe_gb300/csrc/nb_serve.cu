@@ -33,6 +33,9 @@ namespace {
 // compensation (96), sort and topology scratch (~110), tree cells at twice the
 // measured count with quadrupoles (~400), direct-sum partials.
 constexpr size_t kBytesPerBody = 640;
+// Bodies one batch may hold: its octree must stay below 2^27 cells (about
+// 1.3 cells per body), the traversal's cell-index range.
+constexpr size_t kMaxBatchBodies = (size_t)96 << 20;
 
 struct Job {
     nb_job spec{};
@@ -54,6 +57,7 @@ struct nb_server {
     std::vector<uint64_t> active;   // in batch galaxy order
     nb_batch* batch = nullptr;
     size_t bytes_used = 0;
+    size_t bodies_used = 0;
     float dt = NAN;                 // dt of the active jobs
     double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
@@ -182,7 +186,7 @@ int nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id) {
     j.st.state = 0;
     j.st.submit_s = now_s(s);
     j.st.bytes = job_bytes(*job);
-    if (j.st.bytes > s->prm.memory_budget) j.st.state = -1;   // can never fit
+    if (j.st.bytes > s->prm.memory_budget || job->n > kMaxBatchBodies) j.st.state = -1;   // can never fit
     const uint64_t jid = j.st.id;
     const bool queued = j.st.state == 0;
     s->jobs.emplace(jid, std::move(j));
@@ -207,6 +211,7 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
             j.st.done_s = now_s(s);
             j.galaxy = -1;
             s->bytes_used -= j.st.bytes;
+            s->bodies_used -= j.spec.n;
             changed = true;
         } else {
             keep.push_back(id);
@@ -218,6 +223,7 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
     while (!s->queue.empty() && (int)s->active.size() < s->prm.max_active) {
         Job& j = s->jobs[s->queue.front()];
         if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
+        if (s->bodies_used + j.spec.n > kMaxBatchBodies) break;
         if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
         int rc = generate(j);
         if (rc) return sfail(s, rc, "job generation failed");
@@ -225,6 +231,7 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
         j.st.admit_s = now_s(s);
         j.galaxy = -1;
         s->bytes_used += j.st.bytes;
+        s->bodies_used += j.spec.n;
         s->dt = j.spec.dt;
         s->active.push_back(j.st.id);
         s->queue.pop_front();
@@ -253,16 +260,17 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
         bool generated = false;
         {
             int slots = s->prm.max_active - (int)s->active.size();
-            size_t bytes = s->bytes_used;
+            size_t bytes = s->bytes_used, bodies = s->bodies_used;
             for (uint64_t id : s->queue) {
                 Job& j = s->jobs[id];
                 if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
-                if (j.spec.dt != s->dt) break;
+                if (bodies + j.spec.n > kMaxBatchBodies || j.spec.dt != s->dt) break;
                 generated |= !j.generated;
                 rc = generate(j);
                 if (rc) break;   // reported when the job is admitted
                 --slots;
                 bytes += j.st.bytes;
+                bodies += j.spec.n;
             }
         }
         rc = batch_wait(s->batch);
