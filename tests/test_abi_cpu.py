@@ -141,3 +141,18 @@ def test_seeders_match_golden_inputs():
     np.testing.assert_array_equal(v, g["plummer256_vel"])
     pm, v = nb.seed_disk(5, 512)
     np.testing.assert_array_equal(pm, g["disk512_pos_mass"])
+
+
+def test_server_rejects_jobs_that_can_never_fit():
+    """Admission bounds checked at submission, before any device work: a job
+    larger than the memory budget or than one batch's octree can index is
+    rejected (state -1) and never queued."""
+    import nbody_serve as ns
+    with ns.NBodyServer(memory_budget=640 * 10_000) as s:
+        small = s.submit(1, 5_000, 10, 1e-3, 0)
+        over_budget = s.submit(2, 20_000, 10, 1e-3, 0)
+        assert s.status(small)["state"] == 0
+        assert s.status(over_budget)["state"] == -1
+    with ns.NBodyServer() as s:   # 120 GB budget: 110 M bodies fit it, not one batch's octree
+        too_many = s.submit(3, 110 << 20, 10, 1e-3, 0)
+        assert s.status(too_many)["state"] == -1
