@@ -263,49 +263,48 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
         }
         // the rest: each body decides, as the reference's recursion does
         __syncwarp();
-        for (unsigned rem = bD; rem && !bad; rem &= rem - 1u) {
-            const int j = __ffs(rem) - 1;
+        // Two ambiguous children per iteration: their arithmetic is independent,
+        // so the two dependency chains interleave; the stack receives the first
+        // child's entry before the second's, as one child per iteration would.
+        auto decide = [&](int j, unsigned pm0, unsigned pm1, unsigned chj, bool& open0, bool& open1) {
             const float4 cm = kid_cm[w][j];
             const int4 mt = kid_mt[w][j];
-            const unsigned pm0 = __shfl_sync(0xffffffffu, cm0, j), pm1 = __shfl_sync(0xffffffffu, cm1, j);
-            const unsigned chj = __shfl_sync(0xffffffffu, ch, j);
             const bool a0 = (pm0 >> lane) & 1u, a1 = (pm1 >> lane) & 1u;
-            const int kind = mt.w & 15;
-            bool open0 = false, open1 = false;
-            if (a0 || a1) {
-                // the reference's float distance: dv = p - COM, r2 = (dvx^2 + dvy^2) + dvz^2, each op
-                // rounded; d = COM - p = -dv exactly (rounding is symmetric), so r2 is the same
-                const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
-                const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
-                const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
-                const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                const float thr_acc = __int_as_float(mt.y), thr_rej = __int_as_float(mt.z);
-                bool acc0 = r2.x > thr_acc, acc1 = r2.y > thr_acc;
-                const bool band0 = a0 && !acc0 && !(r2.x < thr_rej), band1 = a1 && !acc1 && !(r2.y < thr_rej);
-                if (band0 || band1) {
-                    const float side = __ldg(&cell_lo[chj]).w;
-                    if (band0) acc0 = __fdiv_rn(side, __fsqrt_rn(r2.x)) < theta_f;
-                    if (band1) acc1 = __fdiv_rn(side, __fsqrt_rn(r2.y)) < theta_f;
-                }
-                acc0 = acc0 && a0;
-                acc1 = acc1 && a1;
-                if ((acc0 || acc1) && cm.w != 0.f) {
-                    pair_accel_x2<LAW>(dx, dy, dz, r2, make_float2(acc0 ? cm.w : 0.f, acc1 ? cm.w : 0.f), S2, tx, ty,
-                                       tz);
-                    cnt += (acc0 ? 1u : 0u) + (acc1 ? 1u : 0u);
-                }
-                if (kind == TK_INTERNAL) {
-                    open0 = a0 && !acc0;
-                    open1 = a1 && !acc1;
-                } else {
-                    // opened depth-cap bucket: each of its bodies except the body itself
-                    const int bc = mt.w >> 8;
-                    if (a0 && !acc0) bucket_accel<LAW>(spos, mt.x, bc, n, s0, p0, S, tx.x, ty.x, tz.x, cnt);
-                    if (a1 && !acc1) bucket_accel<LAW>(spos, mt.x, bc, n, s1, p1, S, tx.y, ty.y, tz.y, cnt);
-                }
+            // the reference's float distance: dv = p - COM, r2 = (dvx^2 + dvy^2) + dvz^2, each op
+            // rounded; d = COM - p = -dv exactly (rounding is symmetric), so r2 is the same
+            const float2 dx = __fadd2_rn(make_float2(cm.x, cm.x), nx);
+            const float2 dy = __fadd2_rn(make_float2(cm.y, cm.y), ny);
+            const float2 dz = __fadd2_rn(make_float2(cm.z, cm.z), nz);
+            const float2 r2 = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+            const float thr_acc = __int_as_float(mt.y), thr_rej = __int_as_float(mt.z);
+            bool acc0 = r2.x > thr_acc, acc1 = r2.y > thr_acc;
+            const bool band0 = a0 && !acc0 && !(r2.x < thr_rej), band1 = a1 && !acc1 && !(r2.y < thr_rej);
+            if (band0 || band1) {
+                const float side = __ldg(&cell_lo[chj]).w;
+                if (band0) acc0 = __fdiv_rn(side, __fsqrt_rn(r2.x)) < theta_f;
+                if (band1) acc1 = __fdiv_rn(side, __fsqrt_rn(r2.y)) < theta_f;
             }
+            acc0 = acc0 && a0;
+            acc1 = acc1 && a1;
+            // a body that does not take the cell adds an exact zero (zero mass, finite factor)
+            pair_accel_x2<LAW>(dx, dy, dz, r2, make_float2(acc0 ? cm.w : 0.f, acc1 ? cm.w : 0.f), S2, tx, ty, tz);
+            if (cm.w != 0.f) cnt += (acc0 ? 1u : 0u) + (acc1 ? 1u : 0u);
+            const int kind = mt.w & 15;
+            if (kind == TK_INTERNAL) {
+                open0 = a0 && !acc0;
+                open1 = a1 && !acc1;
+            } else {
+                // opened depth-cap bucket: each of its bodies except the body itself
+                const int bc = mt.w >> 8;
+                if (a0 && !acc0) bucket_accel<LAW>(spos, mt.x, bc, n, s0, p0, S, tx.x, ty.x, tz.x, cnt);
+                if (a1 && !acc1) bucket_accel<LAW>(spos, mt.x, bc, n, s1, p1, S, tx.y, ty.y, tz.y, cnt);
+                open0 = open1 = false;
+            }
+        };
+        auto push = [&](int j, bool open0, bool open1) {
             const unsigned b0 = __ballot_sync(0xffffffffu, open0), b1 = __ballot_sync(0xffffffffu, open1);
             if (b0 | b1) {
+                const int4 mt = kid_mt[w][j];
                 const unsigned cf = (unsigned)mt.x, cn = ((unsigned)mt.w >> 4) & 15u;
                 if (top < kStack && cf < (1u << kRangeBits) && cn >= 1 && cn <= 8 && cf + cn <= (unsigned)n_cells) {
                     if (lane == 0) stk[w][top] = make_int4((int)(cf | (cn << kRangeBits)), (int)b0, (int)b1, 0);
@@ -314,6 +313,22 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                     bad = true;
                 }
             }
+        };
+        for (unsigned rem = bD; rem && !bad;) {
+            const int j = __ffs(rem) - 1;
+            rem &= rem - 1u;
+            const bool two = rem != 0u;   // warp-uniform
+            const int k = two ? __ffs(rem) - 1 : j;
+            if (two) rem &= rem - 1u;
+            const unsigned pj0 = __shfl_sync(0xffffffffu, cm0, j), pj1 = __shfl_sync(0xffffffffu, cm1, j);
+            const unsigned chj = __shfl_sync(0xffffffffu, ch, j);
+            const unsigned pk0 = __shfl_sync(0xffffffffu, cm0, k), pk1 = __shfl_sync(0xffffffffu, cm1, k);
+            const unsigned chk = __shfl_sync(0xffffffffu, ch, k);
+            bool oj0, oj1, ok0, ok1;
+            decide(j, pj0, pj1, chj, oj0, oj1);
+            decide(k, two ? pk0 : 0u, two ? pk1 : 0u, chk, ok0, ok1);
+            push(j, oj0, oj1);
+            if (two && !bad) push(k, ok0, ok1);
         }
         fold();
         // A well-formed tree pushes each internal cell at most once per warp.
