@@ -173,6 +173,7 @@ def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, t
     makespan = max(s["done_s"] for s in st) - min(s["submit_s"] for s in st)
     total = float(sizes.sum()) * steps
     stats = server.stats()
+    timing = server.timing()
     server.close()
     # sequential plain path: one handle per job (reference per-body Barnes-Hut), FIFO
     def replay(th):
@@ -221,7 +222,7 @@ def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, t
         "offered": {"value": rate * float(sizes.mean()) * steps, "unit": METRIC},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
-        "makespan_s": makespan, "rounds": stats["rounds"],
+        "makespan_s": makespan, "rounds": stats["rounds"], "server_timing": timing,
         "force_rel_l2_vs_fp64_largest": served_err,
         "sequential_plain": {"value": seq_value, "unit": METRIC, "theta": theta,
                              "force_rel_l2_vs_fp64_largest": plain_err,

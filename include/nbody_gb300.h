@@ -351,6 +351,11 @@ int  nb_server_status(nb_server* s, uint64_t id, nb_job_status* out);
 int  nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, size_t n);
 /* Body-steps completed and rounds run since creation. */
 int  nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds);
+/* Where the server's time went: batch rebuilds (count, seconds: new batch,
+ * hand-over, upload, tree sizing), stepping (seconds, steps of the batch), and
+ * host generation of initial conditions (seconds). Any pointer may be NULL. */
+int  nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
+                      double* generate_s);
 
 /* ---- allocation-free direct sum -------------------------------------------- */
 /* No counterpart in the reference.  For callers that must not allocate device

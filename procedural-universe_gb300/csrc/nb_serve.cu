@@ -61,6 +61,8 @@ struct nb_server {
     float dt = NAN;                 // dt of the active jobs
     double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
+    uint64_t rebuilds = 0, batch_steps = 0;           // where the time went
+    double rebuild_s = 0, stepping_s = 0, generate_s = 0;
 };
 
 namespace {
@@ -225,7 +227,9 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
         if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
         if (s->bodies_used + j.spec.n > kMaxBatchBodies) break;
         if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
+        const double t_gen = now_s(s);
         int rc = generate(j);
+        s->generate_s += now_s(s) - t_gen;
         if (rc) return sfail(s, rc, "job generation failed");
         j.st.state = 1;
         j.st.admit_s = now_s(s);
@@ -238,8 +242,11 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
         changed = true;
     }
     if (changed && !s->active.empty()) {
+        const double t_rb = now_s(s);
         int rc = rebuild(s);
         if (rc) return rc;
+        s->rebuild_s += now_s(s) - t_rb;
+        ++s->rebuilds;
     } else if (s->active.empty() && s->batch) {
         nb_batch_destroy(s->batch);
         s->batch = nullptr;
@@ -266,7 +273,9 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
                 if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
                 if (bodies + j.spec.n > kMaxBatchBodies || j.spec.dt != s->dt) break;
                 generated |= !j.generated;
+                const double t_gen = now_s(s);
                 rc = generate(j);
+                s->generate_s += now_s(s) - t_gen;
                 if (rc) break;   // reported when the job is admitted
                 --slots;
                 bytes += j.st.bytes;
@@ -276,7 +285,10 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
         rc = batch_wait(s->batch);
         if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
         // a round that also generated may have outlasted its steps: keep the last clean figure
-        if (!generated || s->step_s == 0) s->step_s = (now_s(s) - t_round) / k;
+        const double t_end = now_s(s);
+        if (!generated || s->step_s == 0) s->step_s = (t_end - t_round) / k;
+        s->stepping_s += t_end - t_round;
+        s->batch_steps += (uint64_t)k;
         for (uint64_t id : s->active) {
             Job& j = s->jobs[id];
             j.st.steps_done += k;
@@ -306,6 +318,17 @@ int nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, s
     if (n != j.spec.n) return sfail(s, NB_EINVAL, "size differs from the job's n");
     if (pos_mass4) std::memcpy(pos_mass4, j.res_pos.data(), 16 * n);
     if (vel4) std::memcpy(vel4, j.res_vel.data(), 16 * n);
+    return NB_OK;
+}
+
+int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
+                     double* generate_s) {
+    if (!s) return NB_EINVAL;
+    if (rebuilds) *rebuilds = s->rebuilds;
+    if (rebuild_s) *rebuild_s = s->rebuild_s;
+    if (batch_steps) *batch_steps = s->batch_steps;
+    if (step_s) *step_s = s->stepping_s;
+    if (generate_s) *generate_s = s->generate_s;
     return NB_OK;
 }
 
