@@ -137,3 +137,50 @@ def test_autotune_picks_a_valid_tuning():
         pm, v = gals[5]
         idx = np.arange(0, pm.shape[0], 17)
         assert O.rel_l2(F[idx], fp64_forces(pm, v, idx)) < BH_FP64_TOL
+
+
+def test_coincident_bodies_and_far_field():
+    """A Plummer sphere with 150 bodies on one point: the coincident bodies end
+    in a depth-cap bucket larger than a traversal group (cut into chunks, and
+    summed body by body where it is opened); the far field's local expansion
+    is on by default and off with eta = 0, both within the error bound."""
+    pm, v = nb.seed_plummer(21, 20000)
+    clump = np.tile(np.array([[0.3, -0.2, 0.1, pm[0, 3]]], np.float32), (150, 1))
+    pm = np.concatenate([pm, clump]).astype(np.float32)
+    v = np.concatenate([v, np.zeros((150, 4), np.float32)]).astype(np.float32)
+    n = pm.shape[0]
+    t = np.concatenate([np.arange(0, 20000, 37), np.arange(20000, n, 7)]).astype(np.int32)
+    ref = fp64_forces(pm, v, t)
+    with make_batch([(pm, v)]) as b:
+        F_far = b.forces(0)
+        b.set_far_field(0.0)
+        F_near = b.forces(0)
+        assert b.info()["interactions"] > 0
+    assert np.all(np.isfinite(F_far)) and np.all(np.isfinite(F_near))
+    assert O.rel_l2(F_far[t], ref) < BH_FP64_TOL
+    assert O.rel_l2(F_near[t], ref) < BH_FP64_TOL
+    assert not np.array_equal(F_far, F_near)   # the expansion was used
+
+
+def test_ragged_galaxy_sizes():
+    """Direct-sum members of 2, 3, 255, 256 and 257 bodies (padded to multiples
+    of 256 in the layout) beside one Barnes-Hut member: each matches its own
+    reference, so padding bodies add nothing and galaxies do not mix."""
+    sizes = [2, 3, 255, 256, 257]
+    gals = [nb.seed_plummer(40 + k, n) for k, n in enumerate(sizes)] + [nb.seed_plummer(49, 9000)]
+    with make_batch(gals) as b:
+        for g, (pm, v) in enumerate(gals):
+            F = b.forces(g)
+            n = pm.shape[0]
+            if n >= 8192:
+                t = np.arange(0, n, 7)
+                assert O.rel_l2(F[t], fp64_forces(pm, v, t)) < BH_FP64_TOL
+            else:
+                assert O.rel_l2(F, plain_direct_forces(pm, v)) < DIRECT_TOL, (g, n)
+
+
+def test_batch_without_galaxies_is_refused():
+    b = nb.NBodyBatch(bh_threshold=8192, bh_theta=0.6, softening2=EPS2)
+    with pytest.raises(nb.NBodyError):
+        b.commit()
+    b.close()
