@@ -52,15 +52,30 @@ def force_error(nb, F, pm, v, eps2, samples=1024, seed=3):
     return float(np.linalg.norm(F[t] - F64) / np.linalg.norm(F64))
 
 
-def plain_theta_for(nb, pm, v, eps2, target=1e-3):
+def plain_theta_for(nb, pm, v, eps2, target=1e-3, refine=4):
     """Largest theta of the plain path (the reference's per-body opening rule)
-    whose force error on this galaxy is within target."""
-    for th in PLAIN_THETAS:
+    whose force error on this galaxy is within target: the first grid value
+    that meets it, then bisection towards the next larger grid value (refine
+    halvings, so the comparator is not flattered by the grid's spacing)."""
+    def err_at(th):
         with nb.NBodySim(kind=nb.SIM_BARNES_HUT, softening2=eps2, theta=th) as s:
             s.init_soa(pm, v)
-            e = force_error(nb, s.compute_forces(), pm, v, eps2)
+            return force_error(nb, s.compute_forces(), pm, v, eps2)
+
+    prev = None
+    for th in PLAIN_THETAS:
+        e = err_at(th)
         if e <= target:
-            return th, e
+            lo, e_lo, hi = th, e, prev
+            for _ in range(refine if hi is not None else 0):
+                mid = round(0.5 * (lo + hi), 4)
+                e_mid = err_at(mid)
+                if e_mid <= target:
+                    lo, e_lo = mid, e_mid
+                else:
+                    hi = mid
+            return lo, e_lo
+        prev = th
     return PLAIN_THETAS[-1], e
 
 
@@ -234,7 +249,8 @@ def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, t
         "sequential_plain_equal_accuracy": {
             "value": eq_value, "unit": METRIC, "theta": th_eq, "force_rel_l2_vs_fp64_largest": err_eq,
             "latency_s": {"p50": float(np.percentile(eq_lat, 50)), "p99": float(np.percentile(eq_lat, 99))},
-            "how": "as sequential_plain, at the largest theta whose force error on the largest job is <= 1e-3"},
+            "how": "as sequential_plain, at the largest theta whose force error on the largest job is <= 1e-3 "
+                   "(grid, then bisection to 0.00125)"},
         "speedup_vs_sequential_plain_equal_accuracy": (total / makespan) / eq_value,
         "cpu_baseline": None,
         "cpu_baseline_note": "not timed for the served stream (hours of CPU work); see the bh1m workload",
@@ -363,7 +379,8 @@ def run_batch(args, nb, torch):
         "speedup_vs_sequential_plain": value / seq,
         "sequential_plain_equal_accuracy": {
             "value": seq_eq, "unit": METRIC, "theta": th_eq, "force_rel_l2_vs_fp64_largest": err_eq,
-            "how": "as sequential_plain, at the largest theta whose force error on the largest galaxy is <= 1e-3"},
+            "how": "as sequential_plain, at the largest theta whose force error on the largest galaxy is <= 1e-3 "
+                   "(grid, then bisection to 0.00125)"},
         "speedup_vs_sequential_plain_equal_accuracy": value / seq_eq,
         "force_rel_l2_vs_fp64_max": max(errs) if errs else None, "force_err_galaxies": len(errs),
         "interactions_per_step": info["interactions"], "tuning": tune,
