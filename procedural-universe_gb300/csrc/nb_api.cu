@@ -329,21 +329,25 @@ int sim_check_state(nb_sim* s) {
 extern "C" {
 
 int nb_default_params(nb_params* p) {
-    if (!p) return NB_EINVAL;
-    std::memset(p, 0, sizeof(*p));
-    p->kind = NB_SIM_BARNES_HUT;
-    p->law = NB_LAW_REFERENCE;
-    p->G = 1.0;
-    p->softening2 = 1e-4;
-    p->theta = 0.5;
-    p->pos_scale = 1.0;
-    p->bounds_half = 4000.0f;
-    p->max_depth = 21;
-    p->leaf_size = 1;
-    p->device = 0;
-    p->stream = nullptr;
-    p->flags = NB_FLAG_NONE;
-    return NB_OK;
+    try {
+        if (!p) return NB_EINVAL;
+        std::memset(p, 0, sizeof(*p));
+        p->kind = NB_SIM_BARNES_HUT;
+        p->law = NB_LAW_REFERENCE;
+        p->G = 1.0;
+        p->softening2 = 1e-4;
+        p->theta = 0.5;
+        p->pos_scale = 1.0;
+        p->bounds_half = 4000.0f;
+        p->max_depth = 21;
+        p->leaf_size = 1;
+        p->device = 0;
+        p->stream = nullptr;
+        p->flags = NB_FLAG_NONE;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 const char* nb_sim_name(int kind) {
@@ -356,65 +360,73 @@ const char* nb_sim_name(int kind) {
 }
 
 int nb_create(const nb_params* params, nb_sim** out) {
-    if (!params || !out) return NB_EINVAL;
-    *out = nullptr;
-    std::string why;
-    if (!params_valid(params, why)) return NB_EINVAL;
-    nb_sim* s = new (std::nothrow) nb_sim();
-    if (!s) return NB_ENOMEM;
-    s->prm = *params;
-    s->dev = params->device;
-    int count = 0;
-    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= params->device || params->device < 0) {
-        cudaGetLastError();
-        delete s;
-        return NB_ECUDA;
-    }
-    if (cudaSetDevice(s->dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->dev) != cudaSuccess) {
-        cudaGetLastError();
-        delete s;
-        return NB_ECUDA;
-    }
-    if (cudaDeviceGetAttribute(&s->pageable_access, cudaDevAttrPageableMemoryAccess, s->dev) != cudaSuccess) {
-        cudaGetLastError();
-        s->pageable_access = 0;
-    }
-    if (params->stream) {
-        s->stream = (cudaStream_t)params->stream;
-    } else {
-        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return NB_ECUDA; }
-        s->own_stream = true;
-    }
-    if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess) {
-        cudaGetLastError();
-        nb_destroy(s);
+    try {
+        if (!params || !out) return NB_EINVAL;
+        *out = nullptr;
+        std::string why;
+        if (!params_valid(params, why)) return NB_EINVAL;
+        nb_sim* s = new (std::nothrow) nb_sim();
+        if (!s) return NB_ENOMEM;
+        s->prm = *params;
+        s->dev = params->device;
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count <= params->device || params->device < 0) {
+            cudaGetLastError();
+            delete s;
+            return NB_ECUDA;
+        }
+        if (cudaSetDevice(s->dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->dev) != cudaSuccess) {
+            cudaGetLastError();
+            delete s;
+            return NB_ECUDA;
+        }
+        if (cudaDeviceGetAttribute(&s->pageable_access, cudaDevAttrPageableMemoryAccess, s->dev) != cudaSuccess) {
+            cudaGetLastError();
+            s->pageable_access = 0;
+        }
+        if (params->stream) {
+            s->stream = (cudaStream_t)params->stream;
+        } else {
+            if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return NB_ECUDA; }
+            s->own_stream = true;
+        }
+        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess) {
+            cudaGetLastError();
+            nb_destroy(s);
+            return NB_ENOMEM;
+        }
+        cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
+        cudaMemsetAsync(s->d_inter, 0, sizeof(unsigned long long), s->stream);
+        *s->h_err = 0;
+        *out = s;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
         return NB_ENOMEM;
     }
-    cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
-    cudaMemsetAsync(s->d_inter, 0, sizeof(unsigned long long), s->stream);
-    *s->h_err = 0;
-    *out = s;
-    return NB_OK;
 }
 
 int nb_destroy(nb_sim* s) {
-    if (!s) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    if (s->stream) cudaStreamSynchronize(s->stream);
-    free_state(s);
-    cudaFree(s->d_stage);
-    if (s->h_stage) cudaFreeHost(s->h_stage);
-    for (auto& p : s->prof.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
-    for (cudaEvent_t e : s->prof.pool) cudaEventDestroy(e);
-    cudaFree(s->dscratch);
-    cudaFree(s->d_err);
-    cudaFree(s->d_inter);
-    if (s->h_err) cudaFreeHost(s->h_err);
-    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
-    delete s;
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        free_state(s);
+        cudaFree(s->d_stage);
+        if (s->h_stage) cudaFreeHost(s->h_stage);
+        for (auto& p : s->prof.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+        for (cudaEvent_t e : s->prof.pool) cudaEventDestroy(e);
+        cudaFree(s->dscratch);
+        cudaFree(s->d_err);
+        cudaFree(s->d_inter);
+        if (s->h_err) cudaFreeHost(s->h_err);
+        if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+        delete s;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 const char* nb_last_error(const nb_sim* s) { return s ? s->err.c_str() : "null handle"; }
@@ -486,273 +498,339 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
 extern "C" {
 
 int nb_init_particles(nb_sim* s, const nb_particle* particles, size_t n) {
-    if (!s) return NB_EINVAL;
-    if (!particles && n) return fail(s, NB_EINVAL, "null particle buffer");
-    return init_records(s, particles, -1, 0, 1.f, n, nullptr);
+    try {
+        if (!s) return NB_EINVAL;
+        if (!particles && n) return fail(s, NB_EINVAL, "null particle buffer");
+        return init_records(s, particles, -1, 0, 1.f, n, nullptr);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_init_seeded(nb_sim* s, int seeder, uint64_t seed, float scale, size_t n, nb_particle* records_out) {
-    if (!s) return NB_EINVAL;
-    if (seeder < 0 || seeder > 2 || !(scale > 0)) return fail(s, NB_EINVAL, "bad seeder or scale");
-    return init_records(s, nullptr, seeder, seed, scale, n, records_out);
+    try {
+        if (!s) return NB_EINVAL;
+        if (seeder < 0 || seeder > 2 || !(scale > 0)) return fail(s, NB_EINVAL, "bad seeder or scale");
+        return init_records(s, nullptr, seeder, seed, scale, n, records_out);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_init_soa(nb_sim* s, const float* pos_mass4, const float* vel4, size_t n) {
-    if (!s) return NB_EINVAL;
-    if ((!pos_mass4 || !vel4) && n) return fail(s, NB_EINVAL, "null buffer");
-    if (n > (size_t)INT32_MAX - kPad) return fail(s, NB_EINVAL, "too many particles");
-    cudaSetDevice(s->dev);
-    int rc = ensure_state(s, n);
-    if (rc) return rc;
-    if (n == 0) return NB_OK;
-    NB_CUDA(s, cudaMemcpyAsync(s->pos, pos_mass4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
-    NB_CUDA(s, cudaMemcpyAsync(s->vel, vel4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
-    k_check_soa<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)n, s->posc, s->velc, s->d_err);
-    NB_CUDA(s, cudaGetLastError());
-    rc = check_device_error(s);
-    if (rc) { s->n = 0; return rc; }
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        if ((!pos_mass4 || !vel4) && n) return fail(s, NB_EINVAL, "null buffer");
+        if (n > (size_t)INT32_MAX - kPad) return fail(s, NB_EINVAL, "too many particles");
+        cudaSetDevice(s->dev);
+        int rc = ensure_state(s, n);
+        if (rc) return rc;
+        if (n == 0) return NB_OK;
+        NB_CUDA(s, cudaMemcpyAsync(s->pos, pos_mass4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+        NB_CUDA(s, cudaMemcpyAsync(s->vel, vel4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+        k_check_soa<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)n, s->posc, s->velc, s->d_err);
+        NB_CUDA(s, cudaGetLastError());
+        rc = check_device_error(s);
+        if (rc) { s->n = 0; return rc; }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_step(nb_sim* s, float dt, int nsteps) {
-    if (!s) return NB_EINVAL;
-    if (nsteps < 0 || !std::isfinite(dt)) return fail(s, NB_EINVAL, "bad dt or nsteps");
-    if (s->n == 0) return NB_OK;
-    cudaSetDevice(s->dev);
-    for (int k = 0; k < nsteps; ++k) {
-        int rc = force_pass(s, dt, true);
-        if (rc) return rc;
+    try {
+        if (!s) return NB_EINVAL;
+        if (nsteps < 0 || !std::isfinite(dt)) return fail(s, NB_EINVAL, "bad dt or nsteps");
+        if (s->n == 0) return NB_OK;
+        cudaSetDevice(s->dev);
+        for (int k = 0; k < nsteps; ++k) {
+            int rc = force_pass(s, dt, true);
+            if (rc) return rc;
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_synchronize(nb_sim* s) {
-    if (!s) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    return check_device_error(s);
+    try {
+        if (!s) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        return check_device_error(s);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_read_state(nb_sim* s, float* pos3, double* vel3, double* force3) {
-    if (!s) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    const size_t n = s->n;
-    if (n == 0) return NB_OK;
-    WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
-    WbRecord* h = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
-    if (!d_wb || !h) return fail(s, NB_ENOMEM, "staging allocation failed");
-    k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
-                                                                        (int)n, 0, d_wb);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_read_state");
-    int rc = check_device_error(s);
-    if (rc) return rc;
-    for (size_t i = 0; i < n; ++i) {
-        if (pos3) { pos3[3 * i] = h[i].pos[0]; pos3[3 * i + 1] = h[i].pos[1]; pos3[3 * i + 2] = h[i].pos[2]; }
-        if (vel3) { vel3[3 * i] = h[i].vel[0]; vel3[3 * i + 1] = h[i].vel[1]; vel3[3 * i + 2] = h[i].vel[2]; }
-        if (force3) { force3[3 * i] = h[i].force[0]; force3[3 * i + 1] = h[i].force[1]; force3[3 * i + 2] = h[i].force[2]; }
+    try {
+        if (!s) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        const size_t n = s->n;
+        if (n == 0) return NB_OK;
+        WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
+        WbRecord* h = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
+        if (!d_wb || !h) return fail(s, NB_ENOMEM, "staging allocation failed");
+        k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
+                                                                            (int)n, 0, d_wb);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "nb_read_state");
+        int rc = check_device_error(s);
+        if (rc) return rc;
+        for (size_t i = 0; i < n; ++i) {
+            if (pos3) { pos3[3 * i] = h[i].pos[0]; pos3[3 * i + 1] = h[i].pos[1]; pos3[3 * i + 2] = h[i].pos[2]; }
+            if (vel3) { vel3[3 * i] = h[i].vel[0]; vel3[3 * i + 1] = h[i].vel[1]; vel3[3 * i + 2] = h[i].vel[2]; }
+            if (force3) { force3[3 * i] = h[i].force[0]; force3[3 * i + 1] = h[i].force[1]; force3[3 * i + 2] = h[i].force[2]; }
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
-int nb_write_back_direct(const nb_sim* s) { return s ? (host_direct(s) ? 1 : 0) : -1; }
+int nb_write_back_direct(const nb_sim* s) {
+    try {
+     return s ? (host_direct(s) ? 1 : 0) : -1; 
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
+}
 
 int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
-    if (!s) return NB_EINVAL;
-    if (n != s->n) return fail(s, NB_EINVAL, "record count differs from the initialised count");
-    if (n == 0) return NB_OK;
-    if (!particles) return fail(s, NB_EINVAL, "null particle buffer");
-    cudaSetDevice(s->dev);
-    const int zero = (s->prm.kind != NB_SIM_BARNES_HUT) && !s->forces_fresh;
-    if (host_direct(s) && ((uintptr_t)particles & 3) == 0) {
-        k_writeback_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
-            s->pos, s->vel, s->velc, s->acc, (int)n, zero, reinterpret_cast<uint32_t*>(particles));
+    try {
+        if (!s) return NB_EINVAL;
+        if (n != s->n) return fail(s, NB_EINVAL, "record count differs from the initialised count");
+        if (n == 0) return NB_OK;
+        if (!particles) return fail(s, NB_EINVAL, "null particle buffer");
+        cudaSetDevice(s->dev);
+        const int zero = (s->prm.kind != NB_SIM_BARNES_HUT) && !s->forces_fresh;
+        if (host_direct(s) && ((uintptr_t)particles & 3) == 0) {
+            k_writeback_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
+                s->pos, s->vel, s->velc, s->acc, (int)n, zero, reinterpret_cast<uint32_t*>(particles));
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
+            return check_device_error(s);
+        }
+        WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
+        WbRecord* h_wb = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
+        if (!d_wb || !h_wb) return fail(s, NB_ENOMEM, "staging allocation failed");
+        k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
+                                                                            (int)n, zero, d_wb);
         cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h_wb, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
-        return check_device_error(s);
-    }
-    WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
-    WbRecord* h_wb = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
-    if (!d_wb || !h_wb) return fail(s, NB_ENOMEM, "staging allocation failed");
-    k_pack_writeback<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->posc, s->vel, s->velc, s->acc,
-                                                                        (int)n, zero, d_wb);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h_wb, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
-    int rc = check_device_error(s);
-    if (rc) return rc;
-    auto scatter = [&](size_t b, size_t end) {
-        for (size_t i = b; i < end; ++i) {
-            nb_particle& p = particles[i];
-            const WbRecord& r = h_wb[i];
-            p.position[0] = r.pos[0]; p.position[1] = r.pos[1]; p.position[2] = r.pos[2];
-            p.velocity[0] = r.vel[0]; p.velocity[1] = r.vel[1]; p.velocity[2] = r.vel[2];
-            p.forces[0] = r.force[0]; p.forces[1] = r.force[1]; p.forces[2] = r.force[2];
+        int rc = check_device_error(s);
+        if (rc) return rc;
+        auto scatter = [&](size_t b, size_t end) {
+            for (size_t i = b; i < end; ++i) {
+                nb_particle& p = particles[i];
+                const WbRecord& r = h_wb[i];
+                p.position[0] = r.pos[0]; p.position[1] = r.pos[1]; p.position[2] = r.pos[2];
+                p.velocity[0] = r.vel[0]; p.velocity[1] = r.vel[1]; p.velocity[2] = r.vel[2];
+                p.forces[0] = r.force[0]; p.forces[1] = r.force[1]; p.forces[2] = r.force[2];
+            }
+        };
+        const size_t kPar = 1 << 17;
+        if (n >= 2 * kPar) {
+            unsigned hc = std::max(2u, std::min(16u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> th;
+            const size_t per = (n + hc - 1) / hc;
+            for (unsigned t = 0; t < hc; ++t) {
+                const size_t b = t * per, end = std::min(n, b + per);
+                if (b < end) th.emplace_back(scatter, b, end);
+            }
+            for (auto& x : th) x.join();
+        } else {
+            scatter(0, n);
         }
-    };
-    const size_t kPar = 1 << 17;
-    if (n >= 2 * kPar) {
-        unsigned hc = std::max(2u, std::min(16u, std::thread::hardware_concurrency()));
-        std::vector<std::thread> th;
-        const size_t per = (n + hc - 1) / hc;
-        for (unsigned t = 0; t < hc; ++t) {
-            const size_t b = t * per, end = std::min(n, b + per);
-            if (b < end) th.emplace_back(scatter, b, end);
-        }
-        for (auto& x : th) x.join();
-    } else {
-        scatter(0, n);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_compute_forces(nb_sim* s, double* force3) {
-    if (!s) return NB_EINVAL;
-    if (s->n == 0) return NB_OK;
-    cudaSetDevice(s->dev);
-    int rc = force_pass(s, 0.f, false);
-    if (rc) return rc;
-    if (!force3) return check_device_error(s);
-    return nb_read_state(s, nullptr, nullptr, force3);
+    try {
+        if (!s) return NB_EINVAL;
+        if (s->n == 0) return NB_OK;
+        cudaSetDevice(s->dev);
+        int rc = force_pass(s, 0.f, false);
+        if (rc) return rc;
+        if (!force3) return check_device_error(s);
+        return nb_read_state(s, nullptr, nullptr, force3);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_last_interactions(nb_sim* s, uint64_t* interactions) {
-    if (!s || !interactions) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    if (s->prm.kind == NB_SIM_BARNES_HUT && s->tree.interactions) {
-        unsigned long long v = 0;
-        NB_CUDA(s, cudaMemcpyAsync(&v, s->tree.interactions, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
-        NB_CUDA(s, cudaStreamSynchronize(s->stream));
-        s->inter_last = v;
+    try {
+        if (!s || !interactions) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        if (s->prm.kind == NB_SIM_BARNES_HUT && s->tree.interactions) {
+            unsigned long long v = 0;
+            NB_CUDA(s, cudaMemcpyAsync(&v, s->tree.interactions, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+            NB_CUDA(s, cudaStreamSynchronize(s->stream));
+            s->inter_last = v;
+        }
+        *interactions = s->inter_last;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    *interactions = s->inter_last;
-    return NB_OK;
 }
 
 int nb_fp64_forces(nb_sim* s, const int32_t* targets, size_t m, double* force3) {
-    if (!s) return NB_EINVAL;
-    if (m == 0) return NB_OK;
-    if (!targets || !force3) return fail(s, NB_EINVAL, "null buffer");
-    for (size_t k = 0; k < m; ++k)
-        if (targets[k] < 0 || (size_t)targets[k] >= s->n) return fail(s, NB_EINVAL, "target index out of range");
-    cudaSetDevice(s->dev);
-    int32_t* d_t = nullptr;
-    double* d_o = nullptr;
-    NB_CUDA(s, cudaMallocAsync(&d_t, m * sizeof(int32_t), s->stream));
-    NB_CUDA(s, cudaMallocAsync(&d_o, m * 3 * sizeof(double), s->stream));
-    cudaError_t e = cudaMemcpyAsync(d_t, targets, m * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = fp64_forces(s, d_t, m, d_o);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(force3, d_o, m * 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(d_t, s->stream);
-    cudaFreeAsync(d_o, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_fp64_forces");
-    return check_device_error(s);
+    try {
+        if (!s) return NB_EINVAL;
+        if (m == 0) return NB_OK;
+        if (!targets || !force3) return fail(s, NB_EINVAL, "null buffer");
+        for (size_t k = 0; k < m; ++k)
+            if (targets[k] < 0 || (size_t)targets[k] >= s->n) return fail(s, NB_EINVAL, "target index out of range");
+        cudaSetDevice(s->dev);
+        int32_t* d_t = nullptr;
+        double* d_o = nullptr;
+        NB_CUDA(s, cudaMallocAsync(&d_t, m * sizeof(int32_t), s->stream));
+        NB_CUDA(s, cudaMallocAsync(&d_o, m * 3 * sizeof(double), s->stream));
+        cudaError_t e = cudaMemcpyAsync(d_t, targets, m * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = fp64_forces(s, d_t, m, d_o);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(force3, d_o, m * 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+        cudaFreeAsync(d_t, s->stream);
+        cudaFreeAsync(d_o, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "nb_fp64_forces");
+        return check_device_error(s);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_diagnostics(nb_sim* s, float half_kick_dt, nb_diag* out) {
-    if (!s || !out) return NB_EINVAL;
-    std::memset(out, 0, sizeof(*out));
-    if (s->n == 0) return NB_OK;
-    cudaSetDevice(s->dev);
-    if (half_kick_dt != 0.f) {
-        int rc = force_pass(s, 0.f, false);   // acceleration at the current positions
-        if (rc) return rc;
+    try {
+        if (!s || !out) return NB_EINVAL;
+        std::memset(out, 0, sizeof(*out));
+        if (s->n == 0) return NB_OK;
+        cudaSetDevice(s->dev);
+        if (half_kick_dt != 0.f) {
+            int rc = force_pass(s, 0.f, false);   // acceleration at the current positions
+            if (rc) return rc;
+        }
+        double* d_o = nullptr;
+        double h[16] = {0};
+        NB_CUDA(s, cudaMallocAsync(&d_o, 16 * sizeof(double), s->stream));
+        cudaError_t e = fp64_diagnostics_ex(s, half_kick_dt, half_kick_dt != 0.f, true, d_o);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_o, 12 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+        cudaFreeAsync(d_o, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "nb_diagnostics");
+        out->kinetic = h[0];
+        out->potential = h[11];
+        out->total = h[0] + h[11];
+        out->momentum[0] = h[1]; out->momentum[1] = h[2]; out->momentum[2] = h[3];
+        out->angular_momentum[0] = h[4]; out->angular_momentum[1] = h[5]; out->angular_momentum[2] = h[6];
+        out->mass = h[7];
+        for (int k = 0; k < 3; ++k) out->centre_of_mass[k] = h[7] != 0.0 ? h[8 + k] / h[7] : 0.0;
+        return check_device_error(s);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    double* d_o = nullptr;
-    double h[16] = {0};
-    NB_CUDA(s, cudaMallocAsync(&d_o, 16 * sizeof(double), s->stream));
-    cudaError_t e = fp64_diagnostics_ex(s, half_kick_dt, half_kick_dt != 0.f, true, d_o);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d_o, 12 * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
-    cudaFreeAsync(d_o, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_diagnostics");
-    out->kinetic = h[0];
-    out->potential = h[11];
-    out->total = h[0] + h[11];
-    out->momentum[0] = h[1]; out->momentum[1] = h[2]; out->momentum[2] = h[3];
-    out->angular_momentum[0] = h[4]; out->angular_momentum[1] = h[5]; out->angular_momentum[2] = h[6];
-    out->mass = h[7];
-    for (int k = 0; k < 3; ++k) out->centre_of_mass[k] = h[7] != 0.0 ? h[8 + k] / h[7] : 0.0;
-    return check_device_error(s);
 }
 
 int nb_render_vertices(nb_sim* s, const float* colour4, float scale, nb_render_vertex* out, size_t n) {
-    if (!s || !out) return NB_EINVAL;
-    if (n != s->n) return fail(s, NB_EINVAL, "vertex count differs from the initialised count");
-    if (n == 0) return NB_OK;
-    cudaSetDevice(s->dev);
-    float4* d_c = nullptr;
-    nb_render_vertex* d_v = nullptr;
-    NB_CUDA(s, cudaMallocAsync(&d_v, n * sizeof(nb_render_vertex), s->stream));
-    cudaError_t e = cudaSuccess;
-    if (colour4) {
-        e = cudaMallocAsync(&d_c, n * sizeof(float4), s->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, colour4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+    try {
+        if (!s || !out) return NB_EINVAL;
+        if (n != s->n) return fail(s, NB_EINVAL, "vertex count differs from the initialised count");
+        if (n == 0) return NB_OK;
+        cudaSetDevice(s->dev);
+        float4* d_c = nullptr;
+        nb_render_vertex* d_v = nullptr;
+        NB_CUDA(s, cudaMallocAsync(&d_v, n * sizeof(nb_render_vertex), s->stream));
+        cudaError_t e = cudaSuccess;
+        if (colour4) {
+            e = cudaMallocAsync(&d_c, n * sizeof(float4), s->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, colour4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+        }
+        if (e == cudaSuccess) {
+            k_render_fill<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, d_c, scale, (int)n, d_v);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_v, n * sizeof(nb_render_vertex), cudaMemcpyDeviceToHost, s->stream);
+        if (d_c) cudaFreeAsync(d_c, s->stream);
+        cudaFreeAsync(d_v, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "nb_render_vertices");
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    if (e == cudaSuccess) {
-        k_render_fill<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, d_c, scale, (int)n, d_v);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_v, n * sizeof(nb_render_vertex), cudaMemcpyDeviceToHost, s->stream);
-    if (d_c) cudaFreeAsync(d_c, s->stream);
-    cudaFreeAsync(d_v, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return cuda_fail(s, e, "nb_render_vertices");
-    return NB_OK;
 }
 
 int nb_render_attach(nb_sim* s, const float* colour4, float scale, void** device_vertices) {
-    if (!s || !device_vertices) return NB_EINVAL;
-    if (s->n == 0) return fail(s, NB_EBADSTATE, "nb_init_* first");
-    cudaSetDevice(s->dev);
-    detach_render(s);
-    const size_t n = s->n;
-    NB_CUDA(s, cudaMalloc(&s->render, n * sizeof(nb_render_vertex)));
-    cudaError_t e = cudaMalloc(&s->rcolour, n * sizeof(float4));
-    if (e == cudaSuccess) {
-        if (colour4) {
-            e = cudaMemcpyAsync(s->rcolour, colour4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
-        } else {
-            std::vector<float4> white(n, make_float4(1.f, 1.f, 1.f, 1.f));
-            e = cudaMemcpyAsync(s->rcolour, white.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);   // before `white` goes away
-        }
-    }
-    if (e == cudaSuccess) {
-        s->rscale = scale;
-        k_render_fill<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->rcolour, scale, (int)n,
-                                                                         s->render);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) {
+    try {
+        if (!s || !device_vertices) return NB_EINVAL;
+        if (s->n == 0) return fail(s, NB_EBADSTATE, "nb_init_* first");
+        cudaSetDevice(s->dev);
         detach_render(s);
-        return cuda_fail(s, e, "nb_render_attach");
+        const size_t n = s->n;
+        NB_CUDA(s, cudaMalloc(&s->render, n * sizeof(nb_render_vertex)));
+        cudaError_t e = cudaMalloc(&s->rcolour, n * sizeof(float4));
+        if (e == cudaSuccess) {
+            if (colour4) {
+                e = cudaMemcpyAsync(s->rcolour, colour4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+            } else {
+                std::vector<float4> white(n, make_float4(1.f, 1.f, 1.f, 1.f));
+                e = cudaMemcpyAsync(s->rcolour, white.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);   // before `white` goes away
+            }
+        }
+        if (e == cudaSuccess) {
+            s->rscale = scale;
+            k_render_fill<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->rcolour, scale, (int)n,
+                                                                             s->render);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            detach_render(s);
+            return cuda_fail(s, e, "nb_render_attach");
+        }
+        *device_vertices = s->render;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    *device_vertices = s->render;
-    return NB_OK;
 }
 
 int nb_render_detach(nb_sim* s) {
-    if (!s) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    cudaStreamSynchronize(s->stream);
-    detach_render(s);
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        cudaStreamSynchronize(s->stream);
+        detach_render(s);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_render_read(nb_sim* s, nb_render_vertex* out, size_t n) {
-    if (!s || (!out && n)) return NB_EINVAL;
-    if (!s->render) return fail(s, NB_EBADSTATE, "no vertex buffer attached");
-    if (n != s->n) return fail(s, NB_EINVAL, "vertex count differs from the initialised count");
-    cudaSetDevice(s->dev);
-    NB_CUDA(s, cudaMemcpyAsync(out, s->render, n * sizeof(nb_render_vertex), cudaMemcpyDeviceToHost, s->stream));
-    NB_CUDA(s, cudaStreamSynchronize(s->stream));
-    return NB_OK;
+    try {
+        if (!s || (!out && n)) return NB_EINVAL;
+        if (!s->render) return fail(s, NB_EBADSTATE, "no vertex buffer attached");
+        if (n != s->n) return fail(s, NB_EINVAL, "vertex count differs from the initialised count");
+        cudaSetDevice(s->dev);
+        NB_CUDA(s, cudaMemcpyAsync(out, s->render, n * sizeof(nb_render_vertex), cudaMemcpyDeviceToHost, s->stream));
+        NB_CUDA(s, cudaStreamSynchronize(s->stream));
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"
@@ -821,57 +899,73 @@ __global__ void k_fma_probe(float* out, int iters, float a, float b) {
 extern "C" {
 
 int nb_profile_enable(nb_sim* s, int on) {
-    if (!s) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    nb::drain_profile(s);
-    s->prof.on = on != 0;
-    if (on) {
-        for (int k = 0; k < nb::kPhases; ++k) { s->prof.ms[k] = 0.0; s->prof.count[k] = 0; }
+    try {
+        if (!s) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        nb::drain_profile(s);
+        s->prof.on = on != 0;
+        if (on) {
+            for (int k = 0; k < nb::kPhases; ++k) { s->prof.ms[k] = 0.0; s->prof.count[k] = 0; }
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_profile_read(nb_sim* s, int phase, double* total_ms, uint64_t* launches) {
-    if (!s || phase < 0 || phase >= nb::kPhases) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    nb::drain_profile(s);
-    if (total_ms) *total_ms = s->prof.ms[phase];
-    if (launches) *launches = s->prof.count[phase];
-    return NB_OK;
+    try {
+        if (!s || phase < 0 || phase >= nb::kPhases) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        nb::drain_profile(s);
+        if (total_ms) *total_ms = s->prof.ms[phase];
+        if (launches) *launches = s->prof.count[phase];
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_launch_count(nb_sim* s, uint64_t* launches) {
-    if (!s || !launches) return NB_EINVAL;
-    *launches = s->prof.launches;
-    return NB_OK;
+    try {
+        if (!s || !launches) return NB_EINVAL;
+        *launches = s->prof.launches;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_probe_fp32_peak(int device, double* tflops) {
-    if (!tflops) return NB_EINVAL;
-    *tflops = 0.0;
-    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    float* d = nullptr;
-    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
-    cudaEvent_t a, b;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    const int threads = 512, blocks = sms * 4, iters = 4096;
-    nb::k_fma_probe<<<blocks, threads>>>(d, 64, 1.0000001f, 1e-7f);   // warm-up
-    cudaEventRecord(a);
-    nb::k_fma_probe<<<blocks, threads>>>(d, iters, 1.0000001f, 1e-7f);
-    cudaEventRecord(b);
-    cudaError_t e = cudaEventSynchronize(b);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    cudaFree(d);
-    if (e != cudaSuccess || ms <= 0.f) { cudaGetLastError(); return NB_ECUDA; }
-    const double flops = 2.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
-    *tflops = flops / (ms * 1e-3) / 1e12;
-    return NB_OK;
+    try {
+        if (!tflops) return NB_EINVAL;
+        *tflops = 0.0;
+        if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        float* d = nullptr;
+        if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) { cudaGetLastError(); return NB_ECUDA; }
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        const int threads = 512, blocks = sms * 4, iters = 4096;
+        nb::k_fma_probe<<<blocks, threads>>>(d, 64, 1.0000001f, 1e-7f);   // warm-up
+        cudaEventRecord(a);
+        nb::k_fma_probe<<<blocks, threads>>>(d, iters, 1.0000001f, 1e-7f);
+        cudaEventRecord(b);
+        cudaError_t e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        cudaFree(d);
+        if (e != cudaSuccess || ms <= 0.f) { cudaGetLastError(); return NB_ECUDA; }
+        const double flops = 2.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
+        *tflops = flops / (ms * 1e-3) / 1e12;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"
@@ -879,33 +973,41 @@ int nb_probe_fp32_peak(int device, double* tflops) {
 extern "C" {
 
 int nb_tune(nb_sim* s, const char* key, int value) {
-    if (!s || !key) return NB_EINVAL;
-    const std::string k(key);
-    if (k == "direct_block") {
-        if (value != 64 && value != 128 && value != 256) return NB_EINVAL;
-        s->tune.block = value;
-    } else if (k == "direct_ipt") {
-        if (value != 1 && value != 2 && value != 4 && value != 8) return NB_EINVAL;
-        if (value == 8 && s->tune.block == 256) return NB_EINVAL;
-        s->tune.ipt = value;
-    } else if (k == "direct_splits") {
-        if (value < 0 || value > 4096) return NB_EINVAL;
-        s->tune.splits = value;
-    } else {
-        return NB_EINVAL;
+    try {
+        if (!s || !key) return NB_EINVAL;
+        const std::string k(key);
+        if (k == "direct_block") {
+            if (value != 64 && value != 128 && value != 256) return NB_EINVAL;
+            s->tune.block = value;
+        } else if (k == "direct_ipt") {
+            if (value != 1 && value != 2 && value != 4 && value != 8) return NB_EINVAL;
+            if (value == 8 && s->tune.block == 256) return NB_EINVAL;
+            s->tune.ipt = value;
+        } else if (k == "direct_splits") {
+            if (value < 0 || value > 4096) return NB_EINVAL;
+            s->tune.splits = value;
+        } else {
+            return NB_EINVAL;
+        }
+        s->tune_set = true;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    s->tune_set = true;
-    return NB_OK;
 }
 
 int nb_get_tune(nb_sim* s, const char* key, int* value) {
-    if (!s || !key || !value) return NB_EINVAL;
-    const std::string k(key);
-    if (k == "direct_block") *value = s->tune.block;
-    else if (k == "direct_ipt") *value = s->tune.ipt;
-    else if (k == "direct_splits") *value = s->tune.splits;
-    else return NB_EINVAL;
-    return NB_OK;
+    try {
+        if (!s || !key || !value) return NB_EINVAL;
+        const std::string k(key);
+        if (k == "direct_block") *value = s->tune.block;
+        else if (k == "direct_ipt") *value = s->tune.ipt;
+        else if (k == "direct_splits") *value = s->tune.splits;
+        else return NB_EINVAL;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"

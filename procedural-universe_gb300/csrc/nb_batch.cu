@@ -403,45 +403,53 @@ int batch_wait(nb_batch* b) {
 extern "C" {
 
 int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta, nb_batch** out) {
-    if (!base || !out) return NB_EINVAL;
-    *out = nullptr;
-    if (!(bh_theta > 0) || !std::isfinite(bh_theta) || bh_threshold < 2) return NB_EINVAL;
-    nb_params p = *base;
-    p.kind = NB_SIM_BARNES_HUT;
-    nb_sim* core = nullptr;
-    int rc = nb_create(&p, &core);
-    if (rc) return rc;
-    nb_batch* b = new (std::nothrow) nb_batch();
-    if (!b) {
-        nb_destroy(core);
+    try {
+        if (!base || !out) return NB_EINVAL;
+        *out = nullptr;
+        if (!(bh_theta > 0) || !std::isfinite(bh_theta) || bh_threshold < 2) return NB_EINVAL;
+        nb_params p = *base;
+        p.kind = NB_SIM_BARNES_HUT;
+        nb_sim* core = nullptr;
+        int rc = nb_create(&p, &core);
+        if (rc) return rc;
+        nb_batch* b = new (std::nothrow) nb_batch();
+        if (!b) {
+            nb_destroy(core);
+            return NB_ENOMEM;
+        }
+        b->base = p;
+        b->bh_threshold = bh_threshold;
+        b->bh_theta = bh_theta;
+        b->far_eta = 0.025 / (bh_theta * bh_theta * bh_theta);
+        b->core = core;
+        if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            nb_batch_destroy(b);
+            return NB_ENOMEM;
+        }
+        *out = b;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
         return NB_ENOMEM;
     }
-    b->base = p;
-    b->bh_threshold = bh_threshold;
-    b->bh_theta = bh_theta;
-    b->far_eta = 0.025 / (bh_theta * bh_theta * bh_theta);
-    b->core = core;
-    if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
-        cudaGetLastError();
-        nb_batch_destroy(b);
-        return NB_ENOMEM;
-    }
-    *out = b;
-    return NB_OK;
 }
 
 int nb_batch_destroy(nb_batch* b) {
-    if (!b) return NB_EINVAL;
-    if (b->core) cudaSetDevice(b->core->dev);
-    if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
-                    b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
-                    b->unit_comp, b->part, b->next_unit};
-    for (void* p : ptrs) cudaFree(p);
-    if (b->core) nb_destroy(b->core);
-    delete b;
-    return NB_OK;
+    try {
+        if (!b) return NB_EINVAL;
+        if (b->core) cudaSetDevice(b->core->dev);
+        if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
+                        b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
+                        b->unit_comp, b->part, b->next_unit};
+        for (void* p : ptrs) cudaFree(p);
+        if (b->core) nb_destroy(b->core);
+        delete b;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 const char* nb_batch_last_error(const nb_batch* b) { return b ? b->err.c_str() : "null handle"; }
@@ -449,285 +457,329 @@ const char* nb_batch_last_error(const nb_batch* b) { return b ? b->err.c_str() :
 void* nb_batch_stream(nb_batch* b) { return b && b->core ? (void*)b->core->stream : nullptr; }
 
 int nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t n, int32_t* galaxy) {
-    if (!b || !pos_mass4 || !vel4 || n == 0) return NB_EINVAL;
-    if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
-    if (n > (1u << 24)) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
-    b->h_pos.emplace_back(pos_mass4, pos_mass4 + 4 * n);
-    b->h_vel.emplace_back(vel4, vel4 + 4 * n);
-    nb_batch::Gal g;
-    g.n = n;
-    g.bh = n >= b->bh_threshold;
-    b->gal.push_back(g);
-    if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
-    return NB_OK;
+    try {
+        if (!b || !pos_mass4 || !vel4 || n == 0) return NB_EINVAL;
+        if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
+        if (n > (1u << 24)) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
+        b->h_pos.emplace_back(pos_mass4, pos_mass4 + 4 * n);
+        b->h_vel.emplace_back(vel4, vel4 + 4 * n);
+        nb_batch::Gal g;
+        g.n = n;
+        g.bh = n >= b->bh_threshold;
+        b->gal.push_back(g);
+        if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_batch_commit(nb_batch* b) {
-    if (!b) return NB_EINVAL;
-    if (b->committed) return bfail(b, NB_EBADSTATE, "already committed");
-    if (b->gal.empty()) return bfail(b, NB_EINVAL, "no galaxies");
-    cudaSetDevice(b->core->dev);
-    // layout: Barnes-Hut galaxies packed first (slot order), then direct-sum
-    // galaxies padded to multiples of 256 bodies
-    size_t off = 0;
-    int slot = 0;
-    for (auto& g : b->gal)
-        if (g.bh) {
-            g.off = off;
-            g.idx = slot++;
-            g.n_pad = g.n;
-            off += g.n;
+    try {
+        if (!b) return NB_EINVAL;
+        if (b->committed) return bfail(b, NB_EBADSTATE, "already committed");
+        if (b->gal.empty()) return bfail(b, NB_EINVAL, "no galaxies");
+        cudaSetDevice(b->core->dev);
+        // layout: Barnes-Hut galaxies packed first (slot order), then direct-sum
+        // galaxies padded to multiples of 256 bodies
+        size_t off = 0;
+        int slot = 0;
+        for (auto& g : b->gal)
+            if (g.bh) {
+                g.off = off;
+                g.idx = slot++;
+                g.n_pad = g.n;
+                off += g.n;
+            }
+        b->n_bh = off;
+        b->nslot = slot;
+        if (slot >= (1 << 21)) return bfail(b, NB_EINVAL, "too many Barnes-Hut galaxies");
+        off = pad_up(off, 256);
+        b->dir_begin = off;
+        int dgi = 0;
+        for (auto& g : b->gal)
+            if (!g.bh) {
+                g.off = off;
+                g.idx = dgi++;
+                g.n_pad = pad_up(g.n, 256);
+                off += g.n_pad;
+                b->direct_pairs += (uint64_t)g.n * (uint64_t)(g.n - 1);
+            }
+        b->ndgal = dgi;
+        b->n_total = off;
+        if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
+        std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
+        std::vector<int4> gal_range(b->nslot);
+        b->n_real = 0;
+        // state: zeroed arrays (padding bodies are zero-mass at the origin), host
+        // galaxies copied in and validated
+        int rc = sim_reserve_zeroed(b->core, b->n_total);
+        if (rc) return bfail(b, rc, nb_last_error(b->core));
+        for (size_t k = 0; k < b->gal.size(); ++k) {
+            const auto& g = b->gal[k];
+            if (!g.dsrc[0]) {
+                NB_BCUDA(b, cudaMemcpyAsync(b->core->pos + g.off, b->h_pos[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
+                                            b->core->stream));
+                NB_BCUDA(b, cudaMemcpyAsync(b->core->vel + g.off, b->h_vel[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
+                                            b->core->stream));
+            }
+            b->n_real += g.n;
+            if (g.bh) {
+                for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
+                slot_start[g.idx] = (int)g.off;
+                gal_range[g.idx] = make_int4((int)g.off, (int)g.n, 0, 0);
+            } else {
+                for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
+            }
         }
-    b->n_bh = off;
-    b->nslot = slot;
-    if (slot >= (1 << 21)) return bfail(b, NB_EINVAL, "too many Barnes-Hut galaxies");
-    off = pad_up(off, 256);
-    b->dir_begin = off;
-    int dgi = 0;
-    for (auto& g : b->gal)
-        if (!g.bh) {
-            g.off = off;
-            g.idx = dgi++;
-            g.n_pad = pad_up(g.n, 256);
-            off += g.n_pad;
-            b->direct_pairs += (uint64_t)g.n * (uint64_t)(g.n - 1);
+        rc = sim_check_state(b->core);
+        if (rc) return bfail(b, rc, nb_last_error(b->core));
+        // galaxies handed over from another batch keep their exact state, compensation included
+        for (const auto& g : b->gal) {
+            if (!g.dsrc[0]) continue;
+            float4* dst[4] = {b->core->pos, b->core->posc, b->core->vel, b->core->velc};
+            for (int a = 0; a < 4; ++a)
+                NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                            b->core->stream));
         }
-    b->ndgal = dgi;
-    b->n_total = off;
-    if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
-    std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
-    std::vector<int4> gal_range(b->nslot);
-    b->n_real = 0;
-    // state: zeroed arrays (padding bodies are zero-mass at the origin), host
-    // galaxies copied in and validated
-    int rc = sim_reserve_zeroed(b->core, b->n_total);
-    if (rc) return bfail(b, rc, nb_last_error(b->core));
-    for (size_t k = 0; k < b->gal.size(); ++k) {
-        const auto& g = b->gal[k];
-        if (!g.dsrc[0]) {
-            NB_BCUDA(b, cudaMemcpyAsync(b->core->pos + g.off, b->h_pos[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
-                                        b->core->stream));
-            NB_BCUDA(b, cudaMemcpyAsync(b->core->vel + g.off, b->h_vel[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
-                                        b->core->stream));
+        NB_BCUDA(b, upload(&b->body_slot, body_slot));
+        NB_BCUDA(b, upload(&b->slot_start, slot_start));
+        NB_BCUDA(b, upload(&b->gal_range, gal_range));
+        NB_BCUDA(b, upload(&b->body_dgal, body_dgal));
+        if (b->nslot > 0) {
+            NB_BCUDA(b, cudaMalloc(&b->gal_box, b->nslot * sizeof(float4)));
+            NB_BCUDA(b, cudaMalloc(&b->gal_root, b->nslot * sizeof(int32_t)));
+            NB_BCUDA(b, cudaMalloc(&b->box_bits, 6 * b->nslot * sizeof(unsigned)));
+            // groups are disjoint and non-empty: at most one per body
+            b->group_cap = (int)b->n_bh;
+            NB_BCUDA(b, cudaMalloc(&b->groups, b->n_bh * sizeof(int4)));
+            NB_BCUDA(b, cudaMalloc(&b->group_ctr, 2 * sizeof(int)));
         }
-        b->n_real += g.n;
-        if (g.bh) {
-            for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
-            slot_start[g.idx] = (int)g.off;
-            gal_range[g.idx] = make_int4((int)g.off, (int)g.n, 0, 0);
-        } else {
-            for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
-        }
+        b->h_pos.clear();
+        b->h_vel.clear();
+        rc = plan_units(b);
+        if (rc) return rc;
+        rc = size_tree(b);
+        if (rc) return rc;
+        b->committed = true;
+        return sync_check(b);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    rc = sim_check_state(b->core);
-    if (rc) return bfail(b, rc, nb_last_error(b->core));
-    // galaxies handed over from another batch keep their exact state, compensation included
-    for (const auto& g : b->gal) {
-        if (!g.dsrc[0]) continue;
-        float4* dst[4] = {b->core->pos, b->core->posc, b->core->vel, b->core->velc};
-        for (int a = 0; a < 4; ++a)
-            NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
-                                        b->core->stream));
-    }
-    NB_BCUDA(b, upload(&b->body_slot, body_slot));
-    NB_BCUDA(b, upload(&b->slot_start, slot_start));
-    NB_BCUDA(b, upload(&b->gal_range, gal_range));
-    NB_BCUDA(b, upload(&b->body_dgal, body_dgal));
-    if (b->nslot > 0) {
-        NB_BCUDA(b, cudaMalloc(&b->gal_box, b->nslot * sizeof(float4)));
-        NB_BCUDA(b, cudaMalloc(&b->gal_root, b->nslot * sizeof(int32_t)));
-        NB_BCUDA(b, cudaMalloc(&b->box_bits, 6 * b->nslot * sizeof(unsigned)));
-        // groups are disjoint and non-empty: at most one per body
-        b->group_cap = (int)b->n_bh;
-        NB_BCUDA(b, cudaMalloc(&b->groups, b->n_bh * sizeof(int4)));
-        NB_BCUDA(b, cudaMalloc(&b->group_ctr, 2 * sizeof(int)));
-    }
-    b->h_pos.clear();
-    b->h_vel.clear();
-    rc = plan_units(b);
-    if (rc) return rc;
-    rc = size_tree(b);
-    if (rc) return rc;
-    b->committed = true;
-    return sync_check(b);
 }
 
 int nb_batch_set_tuning(nb_batch* b, const nb_tuning* t) {
-    if (!b || !t) return NB_EINVAL;
-    if (!tuning_valid(*t)) return bfail(b, NB_EINVAL, "unsupported tuning");
-    b->tune = *t;
-    b->graph_dirty = true;
-    if (!b->committed) return NB_OK;
-    cudaSetDevice(b->core->dev);
-    return plan_units(b);
+    try {
+        if (!b || !t) return NB_EINVAL;
+        if (!tuning_valid(*t)) return bfail(b, NB_EINVAL, "unsupported tuning");
+        b->tune = *t;
+        b->graph_dirty = true;
+        if (!b->committed) return NB_OK;
+        cudaSetDevice(b->core->dev);
+        return plan_units(b);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_batch_set_far_field(nb_batch* b, double eta) {
-    if (!b) return NB_EINVAL;
-    if (!(eta >= 0.0) || eta >= 1.0) return bfail(b, NB_EINVAL, "far-field eta must be in [0, 1)");
-    b->far_eta = eta;
-    b->graph_dirty = true;
-    return NB_OK;
+    try {
+        if (!b) return NB_EINVAL;
+        if (!(eta >= 0.0) || eta >= 1.0) return bfail(b, NB_EINVAL, "far-field eta must be in [0, 1)");
+        b->far_eta = eta;
+        b->graph_dirty = true;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_batch_get_tuning(nb_batch* b, nb_tuning* t) {
-    if (!b || !t) return NB_EINVAL;
-    *t = b->tune;
-    return NB_OK;
+    try {
+        if (!b || !t) return NB_EINVAL;
+        *t = b->tune;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_batch_step(nb_batch* b, float dt, int nsteps) {
-    const int rc = nb::batch_launch_steps(b, dt, nsteps);
-    return rc ? rc : nb::batch_wait(b);
+    try {
+        const int rc = nb::batch_launch_steps(b, dt, nsteps);
+        return rc ? rc : nb::batch_wait(b);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4) {
-    if (!b) return NB_EINVAL;
-    const nb_batch::Gal* g = find(b, galaxy);
-    if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
-    cudaSetDevice(b->core->dev);
-    nb_sim* c = b->core;
-    const size_t n = g->n;
-    std::vector<float4> v(n), vc(n);
-    if (pos_mass4) NB_BCUDA(b, cudaMemcpy(pos_mass4, c->pos + g->off, n * 16, cudaMemcpyDeviceToHost));
-    if (vel4) {
-        NB_BCUDA(b, cudaMemcpy(v.data(), c->vel + g->off, n * 16, cudaMemcpyDeviceToHost));
-        NB_BCUDA(b, cudaMemcpy(vc.data(), c->velc + g->off, n * 16, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < n; ++i) {
-            vel4[4 * i] = (float)((double)v[i].x - vc[i].x);
-            vel4[4 * i + 1] = (float)((double)v[i].y - vc[i].y);
-            vel4[4 * i + 2] = (float)((double)v[i].z - vc[i].z);
-            vel4[4 * i + 3] = 0.f;
+    try {
+        if (!b) return NB_EINVAL;
+        const nb_batch::Gal* g = find(b, galaxy);
+        if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
+        cudaSetDevice(b->core->dev);
+        nb_sim* c = b->core;
+        const size_t n = g->n;
+        std::vector<float4> v(n), vc(n);
+        if (pos_mass4) NB_BCUDA(b, cudaMemcpy(pos_mass4, c->pos + g->off, n * 16, cudaMemcpyDeviceToHost));
+        if (vel4) {
+            NB_BCUDA(b, cudaMemcpy(v.data(), c->vel + g->off, n * 16, cudaMemcpyDeviceToHost));
+            NB_BCUDA(b, cudaMemcpy(vc.data(), c->velc + g->off, n * 16, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < n; ++i) {
+                vel4[4 * i] = (float)((double)v[i].x - vc[i].x);
+                vel4[4 * i + 1] = (float)((double)v[i].y - vc[i].y);
+                vel4[4 * i + 2] = (float)((double)v[i].z - vc[i].z);
+                vel4[4 * i + 3] = 0.f;
+            }
         }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3) {
-    if (!b || !force3) return NB_EINVAL;
-    const nb_batch::Gal* g = find(b, galaxy);
-    if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
-    cudaSetDevice(b->core->dev);
-    int rc = enqueue_step(b, 0.f, false);
-    if (rc) return rc;
-    rc = sync_check(b);
-    if (rc) return rc;
-    nb_sim* c = b->core;
-    std::vector<float4> a(g->n), p(g->n);
-    NB_BCUDA(b, cudaMemcpy(a.data(), c->acc + g->off, g->n * 16, cudaMemcpyDeviceToHost));
-    NB_BCUDA(b, cudaMemcpy(p.data(), c->pos + g->off, g->n * 16, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < g->n; ++i) {
-        const double m = p[i].w;
-        force3[3 * i] = m * a[i].x;
-        force3[3 * i + 1] = m * a[i].y;
-        force3[3 * i + 2] = m * a[i].z;
+    try {
+        if (!b || !force3) return NB_EINVAL;
+        const nb_batch::Gal* g = find(b, galaxy);
+        if (!g || !b->committed) return bfail(b, NB_EINVAL, "unknown galaxy or not committed");
+        cudaSetDevice(b->core->dev);
+        int rc = enqueue_step(b, 0.f, false);
+        if (rc) return rc;
+        rc = sync_check(b);
+        if (rc) return rc;
+        nb_sim* c = b->core;
+        std::vector<float4> a(g->n), p(g->n);
+        NB_BCUDA(b, cudaMemcpy(a.data(), c->acc + g->off, g->n * 16, cudaMemcpyDeviceToHost));
+        NB_BCUDA(b, cudaMemcpy(p.data(), c->pos + g->off, g->n * 16, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < g->n; ++i) {
+            const double m = p[i].w;
+            force3[3 * i] = m * a[i].x;
+            force3[3 * i + 1] = m * a[i].y;
+            force3[3 * i + 2] = m * a[i].z;
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last) {
-    if (!b) return NB_EINVAL;
-    if (galaxies) *galaxies = b->gal.size();
-    if (bodies) *bodies = b->committed ? b->n_real : 0;
-    if (interactions_last) {
-        unsigned long long v = 0;
-        if (b->committed && b->n_bh > 0) {
-            cudaSetDevice(b->core->dev);
-            NB_BCUDA(b, cudaMemcpy(&v, b->core->tree.interactions, sizeof(v), cudaMemcpyDeviceToHost));
+    try {
+        if (!b) return NB_EINVAL;
+        if (galaxies) *galaxies = b->gal.size();
+        if (bodies) *bodies = b->committed ? b->n_real : 0;
+        if (interactions_last) {
+            unsigned long long v = 0;
+            if (b->committed && b->n_bh > 0) {
+                cudaSetDevice(b->core->dev);
+                NB_BCUDA(b, cudaMemcpy(&v, b->core->tree.interactions, sizeof(v), cudaMemcpyDeviceToHost));
+            }
+            *interactions_last = (uint64_t)v + b->direct_pairs;
         }
-        *interactions_last = (uint64_t)v + b->direct_pairs;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_batch_tree_stats(nb_batch* b, int64_t* stats4) {
-    if (!b || !stats4) return NB_EINVAL;
-    for (int k = 0; k < 4; ++k) stats4[k] = 0;
-    if (!b->committed || b->n_bh == 0) return NB_OK;
-    cudaSetDevice(b->core->dev);
-    int32_t h[TC_COUNT];
-    int rc = read_tree_counts(b, h);
-    if (rc) return rc;
-    int ctr[2] = {0, 0};
-    NB_BCUDA(b, cudaMemcpy(ctr, b->group_ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
-    stats4[0] = ctr[0];
-    stats4[1] = h[TC_NINT];
-    stats4[2] = (int64_t)h[TC_NINT] + h[TC_NLEAF];
-    stats4[3] = (int64_t)b->n_bh;
-    return NB_OK;
+    try {
+        if (!b || !stats4) return NB_EINVAL;
+        for (int k = 0; k < 4; ++k) stats4[k] = 0;
+        if (!b->committed || b->n_bh == 0) return NB_OK;
+        cudaSetDevice(b->core->dev);
+        int32_t h[TC_COUNT];
+        int rc = read_tree_counts(b, h);
+        if (rc) return rc;
+        int ctr[2] = {0, 0};
+        NB_BCUDA(b, cudaMemcpy(ctr, b->group_ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
+        stats4[0] = ctr[0];
+        stats4[1] = h[TC_NINT];
+        stats4[2] = (int64_t)h[TC_NINT] + h[TC_NLEAF];
+        stats4[3] = (int64_t)b->n_bh;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 // Project autotuner: candidate leaf sizes for the Barnes-Hut members, then
 // candidate direct-sum tilings, each timed over trial_steps graph replays with
 // CUDA events; the state is restored after every trial.
 int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
-    if (!b) return NB_EINVAL;
-    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
-    if (trial_steps < 1) return bfail(b, NB_EINVAL, "trial_steps >= 1");
-    cudaSetDevice(b->core->dev);
-    nb_sim* c = b->core;
-    const size_t bytes = c->n_pad * sizeof(float4);
-    float4* save = nullptr;
-    NB_BCUDA(b, cudaMalloc(&save, 4 * bytes));
-    auto snapshot = [&](bool restore) {
-        float4* arrs[4] = {c->pos, c->posc, c->vel, c->velc};
-        for (int k = 0; k < 4; ++k) {
-            if (restore) cudaMemcpyAsync(arrs[k], save + k * c->n_pad, bytes, cudaMemcpyDeviceToDevice, c->stream);
-            else cudaMemcpyAsync(save + k * c->n_pad, arrs[k], bytes, cudaMemcpyDeviceToDevice, c->stream);
-        }
-    };
-    snapshot(false);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    auto trial = [&](const nb_tuning& t, float* ms) -> int {
-        int rc = nb_batch_set_tuning(b, &t);
-        if (rc) return rc;
-        rc = build_graph(b, dt);
-        if (rc) return rc;
-        cudaGraphLaunch(b->exec, c->stream);   // warm-up
-        cudaEventRecord(e0, c->stream);
-        for (int k = 0; k < trial_steps; ++k) cudaGraphLaunch(b->exec, c->stream);
-        cudaEventRecord(e1, c->stream);
-        rc = sync_check(b);
-        if (rc) return rc;
-        cudaEventElapsedTime(ms, e0, e1);
-        snapshot(true);
-        return NB_OK;
-    };
-    nb_tuning best = b->tune;
-    float best_ms = INFINITY;
-    int rc = NB_OK;
-    const int leafs[] = {8, 16, 32, 64};
-    for (int ls : (b->n_bh > 0 ? std::vector<int>(leafs, leafs + 4) : std::vector<int>{best.leaf_size})) {
-        nb_tuning t = best;
-        t.leaf_size = ls;
-        float ms = 0.f;
-        rc = trial(t, &ms);
-        if (rc) break;
-        if (ms < best_ms) { best_ms = ms; best = t; }
-    }
-    const int shapes[][3] = {{128, 1, 1024}, {128, 2, 1024}, {64, 1, 1024}, {128, 1, 2048}, {256, 1, 1024}, {128, 2, 2048}};
-    if (!rc && b->ndgal > 0) {
-        const nb_tuning base_t = best;
-        for (const auto& sh : shapes) {
-            nb_tuning t = base_t;
-            t.direct_block = sh[0];
-            t.direct_ipt = sh[1];
-            t.direct_jtile = sh[2];
+    try {
+        if (!b) return NB_EINVAL;
+        if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+        if (trial_steps < 1) return bfail(b, NB_EINVAL, "trial_steps >= 1");
+        cudaSetDevice(b->core->dev);
+        nb_sim* c = b->core;
+        const size_t bytes = c->n_pad * sizeof(float4);
+        float4* save = nullptr;
+        NB_BCUDA(b, cudaMalloc(&save, 4 * bytes));
+        auto snapshot = [&](bool restore) {
+            float4* arrs[4] = {c->pos, c->posc, c->vel, c->velc};
+            for (int k = 0; k < 4; ++k) {
+                if (restore) cudaMemcpyAsync(arrs[k], save + k * c->n_pad, bytes, cudaMemcpyDeviceToDevice, c->stream);
+                else cudaMemcpyAsync(save + k * c->n_pad, arrs[k], bytes, cudaMemcpyDeviceToDevice, c->stream);
+            }
+        };
+        snapshot(false);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        auto trial = [&](const nb_tuning& t, float* ms) -> int {
+            int rc = nb_batch_set_tuning(b, &t);
+            if (rc) return rc;
+            rc = build_graph(b, dt);
+            if (rc) return rc;
+            cudaGraphLaunch(b->exec, c->stream);   // warm-up
+            cudaEventRecord(e0, c->stream);
+            for (int k = 0; k < trial_steps; ++k) cudaGraphLaunch(b->exec, c->stream);
+            cudaEventRecord(e1, c->stream);
+            rc = sync_check(b);
+            if (rc) return rc;
+            cudaEventElapsedTime(ms, e0, e1);
+            snapshot(true);
+            return NB_OK;
+        };
+        nb_tuning best = b->tune;
+        float best_ms = INFINITY;
+        int rc = NB_OK;
+        const int leafs[] = {8, 16, 32, 64};
+        for (int ls : (b->n_bh > 0 ? std::vector<int>(leafs, leafs + 4) : std::vector<int>{best.leaf_size})) {
+            nb_tuning t = best;
+            t.leaf_size = ls;
             float ms = 0.f;
             rc = trial(t, &ms);
             if (rc) break;
             if (ms < best_ms) { best_ms = ms; best = t; }
         }
+        const int shapes[][3] = {{128, 1, 1024}, {128, 2, 1024}, {64, 1, 1024}, {128, 1, 2048}, {256, 1, 1024}, {128, 2, 2048}};
+        if (!rc && b->ndgal > 0) {
+            const nb_tuning base_t = best;
+            for (const auto& sh : shapes) {
+                nb_tuning t = base_t;
+                t.direct_block = sh[0];
+                t.direct_ipt = sh[1];
+                t.direct_jtile = sh[2];
+                float ms = 0.f;
+                rc = trial(t, &ms);
+                if (rc) break;
+                if (ms < best_ms) { best_ms = ms; best = t; }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        snapshot(true);
+        cudaStreamSynchronize(c->stream);
+        cudaFree(save);
+        if (rc) return rc;
+        return nb_batch_set_tuning(b, &best);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    snapshot(true);
-    cudaStreamSynchronize(c->stream);
-    cudaFree(save);
-    if (rc) return rc;
-    return nb_batch_set_tuning(b, &best);
 }
 
 }  // extern "C"
@@ -738,37 +790,45 @@ extern "C" {
 // Uploads the state of every galaxy (galaxies in index order, concatenated:
 // n_bodies x float4 each) from host buffers; the tree and graph are reused.
 int nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4) {
-    if (!b || !pos_mass4 || !vel4) return NB_EINVAL;
-    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
-    cudaSetDevice(b->core->dev);
-    nb_sim* c = b->core;
-    size_t src = 0;
-    for (const auto& g : b->gal) {
-        NB_BCUDA(b, cudaMemcpyAsync(c->pos + g.off, pos_mass4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
-        NB_BCUDA(b, cudaMemcpyAsync(c->vel + g.off, vel4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
-        NB_BCUDA(b, cudaMemsetAsync(c->posc + g.off, 0, g.n * 16, c->stream));
-        NB_BCUDA(b, cudaMemsetAsync(c->velc + g.off, 0, g.n * 16, c->stream));
-        src += g.n;
+    try {
+        if (!b || !pos_mass4 || !vel4) return NB_EINVAL;
+        if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+        cudaSetDevice(b->core->dev);
+        nb_sim* c = b->core;
+        size_t src = 0;
+        for (const auto& g : b->gal) {
+            NB_BCUDA(b, cudaMemcpyAsync(c->pos + g.off, pos_mass4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
+            NB_BCUDA(b, cudaMemcpyAsync(c->vel + g.off, vel4 + 4 * src, g.n * 16, cudaMemcpyHostToDevice, c->stream));
+            NB_BCUDA(b, cudaMemsetAsync(c->posc + g.off, 0, g.n * 16, c->stream));
+            NB_BCUDA(b, cudaMemsetAsync(c->velc + g.off, 0, g.n * 16, c->stream));
+            src += g.n;
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 // Downloads positions+masses (and, if vel4 is not NULL, velocities) of every
 // galaxy into host buffers in the same concatenated order.
 int nb_batch_read_state(nb_batch* b, float* pos_mass4, float* vel4) {
-    if (!b || !pos_mass4) return NB_EINVAL;
-    if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
-    cudaSetDevice(b->core->dev);
-    nb_sim* c = b->core;
-    size_t dst = 0;
-    for (const auto& g : b->gal) {
-        NB_BCUDA(b, cudaMemcpyAsync(pos_mass4 + 4 * dst, c->pos + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
-        if (vel4)
-            NB_BCUDA(b, cudaMemcpyAsync(vel4 + 4 * dst, c->vel + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
-        dst += g.n;
+    try {
+        if (!b || !pos_mass4) return NB_EINVAL;
+        if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
+        cudaSetDevice(b->core->dev);
+        nb_sim* c = b->core;
+        size_t dst = 0;
+        for (const auto& g : b->gal) {
+            NB_BCUDA(b, cudaMemcpyAsync(pos_mass4 + 4 * dst, c->pos + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
+            if (vel4)
+                NB_BCUDA(b, cudaMemcpyAsync(vel4 + 4 * dst, c->vel + g.off, g.n * 16, cudaMemcpyDeviceToHost, c->stream));
+            dst += g.n;
+        }
+        NB_BCUDA(b, cudaStreamSynchronize(c->stream));
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    NB_BCUDA(b, cudaStreamSynchronize(c->stream));
-    return NB_OK;
 }
 
 }  // extern "C"

@@ -107,107 +107,119 @@ void finish(std::vector<double>& x, std::vector<double>& v, std::vector<float>& 
 extern "C" {
 
 int nb_seed_plummer(uint64_t seed, size_t n, double total_mass, double a, float* pos_mass4, float* vel4) {
-    if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
-    if (!(a > 0) || !(total_mass > 0)) return NB_EINVAL;
-    std::vector<double> x(3 * n), v(3 * n);
-    std::vector<float> m(n, (float)(total_mass / (double)n));
-    parallel_for(n, [&](size_t b, size_t e) {
-        for (size_t i = b; i < e; ++i) {
-            BodyRng r(seed, i, 1);
-            plummer_body(r, total_mass, a, &x[3 * i], &v[3 * i]);
-        }
-    });
-    finish(x, v, m, n, pos_mass4, vel4);
-    return NB_OK;
+    try {
+        if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
+        if (!(a > 0) || !(total_mass > 0)) return NB_EINVAL;
+        std::vector<double> x(3 * n), v(3 * n);
+        std::vector<float> m(n, (float)(total_mass / (double)n));
+        parallel_for(n, [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) {
+                BodyRng r(seed, i, 1);
+                plummer_body(r, total_mass, a, &x[3 * i], &v[3 * i]);
+            }
+        });
+        finish(x, v, m, n, pos_mass4, vel4);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_seed_disk(uint64_t seed, size_t n, double total_mass, double rd, double z0, double bulge_frac, double ab,
                  double dispersion, float* pos_mass4, float* vel4) {
-    if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
-    if (!(rd > 0) || !(z0 > 0) || bulge_frac < 0 || bulge_frac >= 1 || !(total_mass > 0)) return NB_EINVAL;
-    if (bulge_frac > 0 && !(ab > 0)) return NB_EINVAL;
-    const size_t nb = (size_t)std::llround(bulge_frac * (double)n);
-    const size_t nd = n - nb;
-    const double Md = total_mass * (1.0 - bulge_frac), Mb = total_mass * bulge_frac;
-    std::vector<double> x(3 * n), v(3 * n);
-    std::vector<float> m(n);
-    const float md = nd ? (float)(Md / (double)nd) : 0.f, mb = nb ? (float)(Mb / (double)nb) : 0.f;
-    parallel_for(n, [&](size_t b, size_t e) {
-        for (size_t i = b; i < e; ++i) {
-            BodyRng r(seed, i, 2);
-            double* xi = &x[3 * i];
-            double* vi = &v[3 * i];
-            if (i < nd) {
-                double R = 0;
-                for (int k = 0; k < 1000; ++k) {
-                    R = -rd * std::log(r.uniform() * r.uniform());
-                    if (R <= 20.0 * rd) break;
+    try {
+        if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
+        if (!(rd > 0) || !(z0 > 0) || bulge_frac < 0 || bulge_frac >= 1 || !(total_mass > 0)) return NB_EINVAL;
+        if (bulge_frac > 0 && !(ab > 0)) return NB_EINVAL;
+        const size_t nb = (size_t)std::llround(bulge_frac * (double)n);
+        const size_t nd = n - nb;
+        const double Md = total_mass * (1.0 - bulge_frac), Mb = total_mass * bulge_frac;
+        std::vector<double> x(3 * n), v(3 * n);
+        std::vector<float> m(n);
+        const float md = nd ? (float)(Md / (double)nd) : 0.f, mb = nb ? (float)(Mb / (double)nb) : 0.f;
+        parallel_for(n, [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) {
+                BodyRng r(seed, i, 2);
+                double* xi = &x[3 * i];
+                double* vi = &v[3 * i];
+                if (i < nd) {
+                    double R = 0;
+                    for (int k = 0; k < 1000; ++k) {
+                        R = -rd * std::log(r.uniform() * r.uniform());
+                        if (R <= 20.0 * rd) break;
+                    }
+                    double z = 0;
+                    for (int k = 0; k < 1000; ++k) {
+                        z = z0 * std::atanh(2.0 * r.uniform() - 1.0);
+                        if (std::fabs(z) <= 10.0 * z0) break;
+                    }
+                    const double ph = 2.0 * kPi * r.uniform();
+                    xi[0] = R * std::cos(ph); xi[1] = R * std::sin(ph); xi[2] = z;
+                    const double menc = Md * (1.0 - (1.0 + R / rd) * std::exp(-R / rd)) + Mb * R * R / ((R + ab) * (R + ab));
+                    const double vc = R > 0 ? std::sqrt(menc / R) : 0.0;
+                    vi[0] = -vc * std::sin(ph) + dispersion * vc * normal(r);
+                    vi[1] = vc * std::cos(ph) + dispersion * vc * normal(r);
+                    vi[2] = dispersion * vc * normal(r);
+                    m[i] = md;
+                } else {
+                    double rad = 0;
+                    const double umax = (100.0 / 101.0) * (100.0 / 101.0);
+                    for (int k = 0; k < 1000; ++k) {
+                        const double u = r.uniform();
+                        if (u > umax) continue;
+                        const double s = std::sqrt(u);
+                        rad = ab * s / (1.0 - s);
+                        break;
+                    }
+                    iso_dir(r, rad, xi);
+                    const double sig = std::sqrt(hernquist_sigma2(std::max(rad, 1e-12), Mb, ab));
+                    const double vesc2 = 2.0 * Mb / (rad + ab);
+                    for (int k = 0; k < 1000; ++k) {
+                        vi[0] = sig * normal(r); vi[1] = sig * normal(r); vi[2] = sig * normal(r);
+                        if (vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2] < 0.9025 * vesc2) break;
+                    }
+                    m[i] = mb;
                 }
-                double z = 0;
-                for (int k = 0; k < 1000; ++k) {
-                    z = z0 * std::atanh(2.0 * r.uniform() - 1.0);
-                    if (std::fabs(z) <= 10.0 * z0) break;
-                }
-                const double ph = 2.0 * kPi * r.uniform();
-                xi[0] = R * std::cos(ph); xi[1] = R * std::sin(ph); xi[2] = z;
-                const double menc = Md * (1.0 - (1.0 + R / rd) * std::exp(-R / rd)) + Mb * R * R / ((R + ab) * (R + ab));
-                const double vc = R > 0 ? std::sqrt(menc / R) : 0.0;
-                vi[0] = -vc * std::sin(ph) + dispersion * vc * normal(r);
-                vi[1] = vc * std::cos(ph) + dispersion * vc * normal(r);
-                vi[2] = dispersion * vc * normal(r);
-                m[i] = md;
-            } else {
-                double rad = 0;
-                const double umax = (100.0 / 101.0) * (100.0 / 101.0);
-                for (int k = 0; k < 1000; ++k) {
-                    const double u = r.uniform();
-                    if (u > umax) continue;
-                    const double s = std::sqrt(u);
-                    rad = ab * s / (1.0 - s);
-                    break;
-                }
-                iso_dir(r, rad, xi);
-                const double sig = std::sqrt(hernquist_sigma2(std::max(rad, 1e-12), Mb, ab));
-                const double vesc2 = 2.0 * Mb / (rad + ab);
-                for (int k = 0; k < 1000; ++k) {
-                    vi[0] = sig * normal(r); vi[1] = sig * normal(r); vi[2] = sig * normal(r);
-                    if (vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2] < 0.9025 * vesc2) break;
-                }
-                m[i] = mb;
             }
-        }
-    });
-    finish(x, v, m, n, pos_mass4, vel4);
-    return NB_OK;
+        });
+        finish(x, v, m, n, pos_mass4, vel4);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_seed_collision(uint64_t seed, size_t n, double a, double separation, double pericentre, float* pos_mass4,
                       float* vel4) {
-    if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
-    if (!(a > 0) || !(separation > 0) || pericentre < 0 || pericentre > separation || n < 2) return NB_EINVAL;
-    const size_t h = n / 2;
-    std::vector<double> x(3 * n), v(3 * n);
-    std::vector<float> m(n);
-    // each sphere has mass 1; relative parabolic orbit of total mass 2 (G = 1)
-    const double Mt = 2.0;
-    const double vrel = std::sqrt(2.0 * Mt / separation);
-    const double vt = std::sqrt(2.0 * Mt * pericentre) / separation;
-    const double vr = -std::sqrt(std::max(0.0, vrel * vrel - vt * vt));
-    const double rel_v[3] = {vr, vt, 0.0};
-    const double rel_x[3] = {separation, 0.0, 0.0};
-    parallel_for(n, [&](size_t b, size_t e) {
-        for (size_t i = b; i < e; ++i) {
-            const bool second = i >= h;
-            const size_t cnt = second ? n - h : h;
-            BodyRng r(seed, i, 3);
-            plummer_body(r, 1.0, a, &x[3 * i], &v[3 * i]);
-            const double sgn = second ? 0.5 : -0.5;
-            for (int k = 0; k < 3; ++k) { x[3 * i + k] += sgn * rel_x[k]; v[3 * i + k] += sgn * rel_v[k]; }
-            m[i] = (float)(1.0 / (double)cnt);
-        }
-    });
-    finish(x, v, m, n, pos_mass4, vel4);
-    return NB_OK;
+    try {
+        if ((!pos_mass4 || !vel4) && n) return NB_EINVAL;
+        if (!(a > 0) || !(separation > 0) || pericentre < 0 || pericentre > separation || n < 2) return NB_EINVAL;
+        const size_t h = n / 2;
+        std::vector<double> x(3 * n), v(3 * n);
+        std::vector<float> m(n);
+        // each sphere has mass 1; relative parabolic orbit of total mass 2 (G = 1)
+        const double Mt = 2.0;
+        const double vrel = std::sqrt(2.0 * Mt / separation);
+        const double vt = std::sqrt(2.0 * Mt * pericentre) / separation;
+        const double vr = -std::sqrt(std::max(0.0, vrel * vrel - vt * vt));
+        const double rel_v[3] = {vr, vt, 0.0};
+        const double rel_x[3] = {separation, 0.0, 0.0};
+        parallel_for(n, [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) {
+                const bool second = i >= h;
+                const size_t cnt = second ? n - h : h;
+                BodyRng r(seed, i, 3);
+                plummer_body(r, 1.0, a, &x[3 * i], &v[3 * i]);
+                const double sgn = second ? 0.5 : -0.5;
+                for (int k = 0; k < 3; ++k) { x[3 * i + k] += sgn * rel_x[k]; v[3 * i + k] += sgn * rel_v[k]; }
+                m[i] = (float)(1.0 / (double)cnt);
+            }
+        });
+        finish(x, v, m, n, pos_mass4, vel4);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"

@@ -140,38 +140,50 @@ int rebuild(nb_server* s) {
 extern "C" {
 
 int nb_server_default_params(nb_server_params* p) {
-    if (!p) return NB_EINVAL;
-    std::memset(p, 0, sizeof(*p));
-    nb_default_params(&p->base);
-    p->base.softening2 = 0.005 * 0.005;
-    p->base.theta = 0.5;
-    p->memory_budget = (size_t)120 << 30;
-    p->max_active = 64;
-    p->steps_per_round = 25;
-    p->bh_threshold = 1024;
-    p->round_seconds = 0.1;
-    return NB_OK;
+    try {
+        if (!p) return NB_EINVAL;
+        std::memset(p, 0, sizeof(*p));
+        nb_default_params(&p->base);
+        p->base.softening2 = 0.005 * 0.005;
+        p->base.theta = 0.5;
+        p->memory_budget = (size_t)120 << 30;
+        p->max_active = 64;
+        p->steps_per_round = 25;
+        p->bh_threshold = 1024;
+        p->round_seconds = 0.1;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_create(const nb_server_params* p, nb_server** out) {
-    if (!p || !out) return NB_EINVAL;
-    *out = nullptr;
-    if (p->max_active < 1 || p->steps_per_round < 1 || p->memory_budget == 0 || p->bh_threshold < 2 ||
-        !(p->base.theta > 0) || !(p->round_seconds >= 0))
-        return NB_EINVAL;
-    nb_server* s = new (std::nothrow) nb_server();
-    if (!s) return NB_ENOMEM;
-    s->prm = *p;
-    s->t0 = std::chrono::steady_clock::now();
-    *out = s;
-    return NB_OK;
+    try {
+        if (!p || !out) return NB_EINVAL;
+        *out = nullptr;
+        if (p->max_active < 1 || p->steps_per_round < 1 || p->memory_budget == 0 || p->bh_threshold < 2 ||
+            !(p->base.theta > 0) || !(p->round_seconds >= 0))
+            return NB_EINVAL;
+        nb_server* s = new (std::nothrow) nb_server();
+        if (!s) return NB_ENOMEM;
+        s->prm = *p;
+        s->t0 = std::chrono::steady_clock::now();
+        *out = s;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_destroy(nb_server* s) {
-    if (!s) return NB_EINVAL;
-    if (s->batch) nb_batch_destroy(s->batch);
-    delete s;
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        if (s->batch) nb_batch_destroy(s->batch);
+        delete s;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 const char* nb_server_last_error(const nb_server* s) { return s ? s->err.c_str() : "null handle"; }
@@ -179,164 +191,188 @@ const char* nb_server_last_error(const nb_server* s) { return s ? s->err.c_str()
 double nb_server_clock(nb_server* s) { return s ? now_s(s) : 0.0; }
 
 int nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id) {
-    if (!s || !job) return NB_EINVAL;
-    if (job->n < 2 || job->steps < 1 || !(job->dt > 0) || (job->model != 0 && job->model != 1))
-        return sfail(s, NB_EINVAL, "bad job");
-    Job j;
-    j.spec = *job;
-    j.st.id = s->next_id++;
-    j.st.state = 0;
-    j.st.submit_s = now_s(s);
-    j.st.bytes = job_bytes(*job);
-    if (j.st.bytes > s->prm.memory_budget || job->n > kMaxBatchBodies) j.st.state = -1;   // can never fit
-    const uint64_t jid = j.st.id;
-    const bool queued = j.st.state == 0;
-    s->jobs.emplace(jid, std::move(j));
-    if (queued) s->queue.push_back(jid);
-    if (id) *id = jid;
-    return NB_OK;
+    try {
+        if (!s || !job) return NB_EINVAL;
+        if (job->n < 2 || job->steps < 1 || !(job->dt > 0) || (job->model != 0 && job->model != 1))
+            return sfail(s, NB_EINVAL, "bad job");
+        Job j;
+        j.spec = *job;
+        j.st.id = s->next_id++;
+        j.st.state = 0;
+        j.st.submit_s = now_s(s);
+        j.st.bytes = job_bytes(*job);
+        if (j.st.bytes > s->prm.memory_budget || job->n > kMaxBatchBodies) j.st.state = -1;   // can never fit
+        const uint64_t jid = j.st.id;
+        const bool queued = j.st.state == 0;
+        s->jobs.emplace(jid, std::move(j));
+        if (queued) s->queue.push_back(jid);
+        if (id) *id = jid;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_tick(nb_server* s, int* active, int* queued) {
-    if (!s) return NB_EINVAL;
-    bool changed = false;
-    // retire finished jobs
-    std::vector<uint64_t> keep;
-    for (uint64_t id : s->active) {
-        Job& j = s->jobs[id];
-        if (j.st.steps_done >= j.spec.steps) {
-            j.res_pos.assign(4 * j.spec.n, 0.f);
-            j.res_vel.assign(4 * j.spec.n, 0.f);
-            int rc = nb_batch_read(s->batch, j.galaxy, j.res_pos.data(), j.res_vel.data());
-            if (rc) return sfail(s, rc, std::string("read result: ") + nb_batch_last_error(s->batch));
-            j.st.state = 2;
-            j.st.done_s = now_s(s);
-            j.galaxy = -1;
-            s->bytes_used -= j.st.bytes;
-            s->bodies_used -= j.spec.n;
-            changed = true;
-        } else {
-            keep.push_back(id);
-        }
-    }
-    s->active.swap(keep);
-    if (s->active.empty()) s->dt = NAN;
-    // admit queued jobs (FIFO) while a slot and the budget allow
-    while (!s->queue.empty() && (int)s->active.size() < s->prm.max_active) {
-        Job& j = s->jobs[s->queue.front()];
-        if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
-        if (s->bodies_used + j.spec.n > kMaxBatchBodies) break;
-        if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
-        const double t_gen = now_s(s);
-        int rc = generate(j);
-        s->generate_s += now_s(s) - t_gen;
-        if (rc) return sfail(s, rc, "job generation failed");
-        j.st.state = 1;
-        j.st.admit_s = now_s(s);
-        j.galaxy = -1;
-        s->bytes_used += j.st.bytes;
-        s->bodies_used += j.spec.n;
-        s->dt = j.spec.dt;
-        s->active.push_back(j.st.id);
-        s->queue.pop_front();
-        changed = true;
-    }
-    if (changed && !s->active.empty()) {
-        const double t_rb = now_s(s);
-        int rc = rebuild(s);
-        if (rc) return rc;
-        s->rebuild_s += now_s(s) - t_rb;
-        ++s->rebuilds;
-    } else if (s->active.empty() && s->batch) {
-        nb_batch_destroy(s->batch);
-        s->batch = nullptr;
-    }
-    // one round
-    if (!s->active.empty()) {
-        int k = s->prm.steps_per_round;
-        for (uint64_t id : s->active) k = std::min(k, s->jobs[id].spec.steps - s->jobs[id].st.steps_done);
-        if (s->prm.round_seconds > 0) {
-            const double fit = s->step_s > 0 ? s->prm.round_seconds / s->step_s : 1.0;
-            if (fit < (double)k) k = (int)fit;
-        }
-        k = std::max(k, 1);
-        const double t_round = now_s(s);
-        int rc = batch_launch_steps(s->batch, s->dt, k);
-        if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
-        // meanwhile: initial conditions of the queued jobs the next admission can take
-        bool generated = false;
-        {
-            int slots = s->prm.max_active - (int)s->active.size();
-            size_t bytes = s->bytes_used, bodies = s->bodies_used;
-            for (uint64_t id : s->queue) {
-                Job& j = s->jobs[id];
-                if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
-                if (bodies + j.spec.n > kMaxBatchBodies || j.spec.dt != s->dt) break;
-                generated |= !j.generated;
-                const double t_gen = now_s(s);
-                rc = generate(j);
-                s->generate_s += now_s(s) - t_gen;
-                if (rc) break;   // reported when the job is admitted
-                --slots;
-                bytes += j.st.bytes;
-                bodies += j.spec.n;
-            }
-        }
-        rc = batch_wait(s->batch);
-        if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
-        // a round that also generated may have outlasted its steps: keep the last clean figure
-        const double t_end = now_s(s);
-        if (!generated || s->step_s == 0) s->step_s = (t_end - t_round) / k;
-        s->stepping_s += t_end - t_round;
-        s->batch_steps += (uint64_t)k;
+    try {
+        if (!s) return NB_EINVAL;
+        bool changed = false;
+        // retire finished jobs
+        std::vector<uint64_t> keep;
         for (uint64_t id : s->active) {
             Job& j = s->jobs[id];
-            j.st.steps_done += k;
-            s->body_steps += (uint64_t)k * j.spec.n;
+            if (j.st.steps_done >= j.spec.steps) {
+                j.res_pos.assign(4 * j.spec.n, 0.f);
+                j.res_vel.assign(4 * j.spec.n, 0.f);
+                int rc = nb_batch_read(s->batch, j.galaxy, j.res_pos.data(), j.res_vel.data());
+                if (rc) return sfail(s, rc, std::string("read result: ") + nb_batch_last_error(s->batch));
+                j.st.state = 2;
+                j.st.done_s = now_s(s);
+                j.galaxy = -1;
+                s->bytes_used -= j.st.bytes;
+                s->bodies_used -= j.spec.n;
+                changed = true;
+            } else {
+                keep.push_back(id);
+            }
         }
-        ++s->rounds;
+        s->active.swap(keep);
+        if (s->active.empty()) s->dt = NAN;
+        // admit queued jobs (FIFO) while a slot and the budget allow
+        while (!s->queue.empty() && (int)s->active.size() < s->prm.max_active) {
+            Job& j = s->jobs[s->queue.front()];
+            if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
+            if (s->bodies_used + j.spec.n > kMaxBatchBodies) break;
+            if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
+            const double t_gen = now_s(s);
+            int rc = generate(j);
+            s->generate_s += now_s(s) - t_gen;
+            if (rc) return sfail(s, rc, "job generation failed");
+            j.st.state = 1;
+            j.st.admit_s = now_s(s);
+            j.galaxy = -1;
+            s->bytes_used += j.st.bytes;
+            s->bodies_used += j.spec.n;
+            s->dt = j.spec.dt;
+            s->active.push_back(j.st.id);
+            s->queue.pop_front();
+            changed = true;
+        }
+        if (changed && !s->active.empty()) {
+            const double t_rb = now_s(s);
+            int rc = rebuild(s);
+            if (rc) return rc;
+            s->rebuild_s += now_s(s) - t_rb;
+            ++s->rebuilds;
+        } else if (s->active.empty() && s->batch) {
+            nb_batch_destroy(s->batch);
+            s->batch = nullptr;
+        }
+        // one round
+        if (!s->active.empty()) {
+            int k = s->prm.steps_per_round;
+            for (uint64_t id : s->active) k = std::min(k, s->jobs[id].spec.steps - s->jobs[id].st.steps_done);
+            if (s->prm.round_seconds > 0) {
+                const double fit = s->step_s > 0 ? s->prm.round_seconds / s->step_s : 1.0;
+                if (fit < (double)k) k = (int)fit;
+            }
+            k = std::max(k, 1);
+            const double t_round = now_s(s);
+            int rc = batch_launch_steps(s->batch, s->dt, k);
+            if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
+            // meanwhile: initial conditions of the queued jobs the next admission can take
+            bool generated = false;
+            {
+                int slots = s->prm.max_active - (int)s->active.size();
+                size_t bytes = s->bytes_used, bodies = s->bodies_used;
+                for (uint64_t id : s->queue) {
+                    Job& j = s->jobs[id];
+                    if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
+                    if (bodies + j.spec.n > kMaxBatchBodies || j.spec.dt != s->dt) break;
+                    generated |= !j.generated;
+                    const double t_gen = now_s(s);
+                    rc = generate(j);
+                    s->generate_s += now_s(s) - t_gen;
+                    if (rc) break;   // reported when the job is admitted
+                    --slots;
+                    bytes += j.st.bytes;
+                    bodies += j.spec.n;
+                }
+            }
+            rc = batch_wait(s->batch);
+            if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
+            // a round that also generated may have outlasted its steps: keep the last clean figure
+            const double t_end = now_s(s);
+            if (!generated || s->step_s == 0) s->step_s = (t_end - t_round) / k;
+            s->stepping_s += t_end - t_round;
+            s->batch_steps += (uint64_t)k;
+            for (uint64_t id : s->active) {
+                Job& j = s->jobs[id];
+                j.st.steps_done += k;
+                s->body_steps += (uint64_t)k * j.spec.n;
+            }
+            ++s->rounds;
+        }
+        if (active) *active = (int)s->active.size();
+        if (queued) *queued = (int)s->queue.size();
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    if (active) *active = (int)s->active.size();
-    if (queued) *queued = (int)s->queue.size();
-    return NB_OK;
 }
 
 int nb_server_status(nb_server* s, uint64_t id, nb_job_status* out) {
-    if (!s || !out) return NB_EINVAL;
-    auto it = s->jobs.find(id);
-    if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
-    *out = it->second.st;
-    return NB_OK;
+    try {
+        if (!s || !out) return NB_EINVAL;
+        auto it = s->jobs.find(id);
+        if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
+        *out = it->second.st;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, size_t n) {
-    if (!s) return NB_EINVAL;
-    auto it = s->jobs.find(id);
-    if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
-    const Job& j = it->second;
-    if (j.st.state != 2) return sfail(s, NB_EBADSTATE, "job not done");
-    if (n != j.spec.n) return sfail(s, NB_EINVAL, "size differs from the job's n");
-    if (pos_mass4) std::memcpy(pos_mass4, j.res_pos.data(), 16 * n);
-    if (vel4) std::memcpy(vel4, j.res_vel.data(), 16 * n);
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        auto it = s->jobs.find(id);
+        if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
+        const Job& j = it->second;
+        if (j.st.state != 2) return sfail(s, NB_EBADSTATE, "job not done");
+        if (n != j.spec.n) return sfail(s, NB_EINVAL, "size differs from the job's n");
+        if (pos_mass4) std::memcpy(pos_mass4, j.res_pos.data(), 16 * n);
+        if (vel4) std::memcpy(vel4, j.res_vel.data(), 16 * n);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
                      double* generate_s) {
-    if (!s) return NB_EINVAL;
-    if (rebuilds) *rebuilds = s->rebuilds;
-    if (rebuild_s) *rebuild_s = s->rebuild_s;
-    if (batch_steps) *batch_steps = s->batch_steps;
-    if (step_s) *step_s = s->stepping_s;
-    if (generate_s) *generate_s = s->generate_s;
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        if (rebuilds) *rebuilds = s->rebuilds;
+        if (rebuild_s) *rebuild_s = s->rebuild_s;
+        if (batch_steps) *batch_steps = s->batch_steps;
+        if (step_s) *step_s = s->stepping_s;
+        if (generate_s) *generate_s = s->generate_s;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds) {
-    if (!s) return NB_EINVAL;
-    if (body_steps) *body_steps = s->body_steps;
-    if (rounds) *rounds = s->rounds;
-    return NB_OK;
+    try {
+        if (!s) return NB_EINVAL;
+        if (body_steps) *body_steps = s->body_steps;
+        if (rounds) *rounds = s->rounds;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"

@@ -115,101 +115,121 @@ int ensure_tree(nb_sim* s) {
 extern "C" {
 
 int nb_tree_keys(nb_sim* s, uint64_t* keys, int32_t* depth) {
-    if (!s || !keys || !depth) return NB_EINVAL;
-    if (s->n == 0) return NB_OK;
-    cudaSetDevice(s->dev);
-    uint64_t* dk = nullptr;
-    int32_t* dd = nullptr;
-    cudaError_t e = cudaMallocAsync(&dk, s->n * 8, s->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dd, s->n * 4, s->stream);
-    if (e == cudaSuccess) e = tree_keys_export(s, dk, dd);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(keys, dk, s->n * 8, cudaMemcpyDeviceToHost, s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(depth, dd, s->n * 4, cudaMemcpyDeviceToHost, s->stream);
-    if (dk) cudaFreeAsync(dk, s->stream);
-    if (dd) cudaFreeAsync(dd, s->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return tfail(s, NB_ECUDA, std::string("nb_tree_keys: ") + cudaGetErrorString(e));
-    return NB_OK;
+    try {
+        if (!s || !keys || !depth) return NB_EINVAL;
+        if (s->n == 0) return NB_OK;
+        cudaSetDevice(s->dev);
+        uint64_t* dk = nullptr;
+        int32_t* dd = nullptr;
+        cudaError_t e = cudaMallocAsync(&dk, s->n * 8, s->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(&dd, s->n * 4, s->stream);
+        if (e == cudaSuccess) e = tree_keys_export(s, dk, dd);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(keys, dk, s->n * 8, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(depth, dd, s->n * 4, cudaMemcpyDeviceToHost, s->stream);
+        if (dk) cudaFreeAsync(dk, s->stream);
+        if (dd) cudaFreeAsync(dd, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return tfail(s, NB_ECUDA, std::string("nb_tree_keys: ") + cudaGetErrorString(e));
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_tree_size(nb_sim* s, size_t* nodes) {
-    if (!s || !nodes) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    int rc = ensure_tree(s);
-    if (rc) return rc;
-    *nodes = s->tree.trivial ? 0 : (size_t)s->tree.n_cells;
-    return NB_OK;
+    try {
+        if (!s || !nodes) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        int rc = ensure_tree(s);
+        if (rc) return rc;
+        *nodes = s->tree.trivial ? 0 : (size_t)s->tree.n_cells;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_tree_stats(nb_sim* s, int64_t* stats8) {
-    if (!s || !stats8) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    int rc = ensure_tree(s);
-    if (rc) return rc;
-    int32_t h[TC_COUNT] = {0};
-    cudaError_t e = cudaMemcpy(h, s->tree.counters, sizeof(h), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return tfail(s, NB_ECUDA, cudaGetErrorString(e));
-    stats8[0] = h[TC_NIN];
-    stats8[1] = s->tree.trivial ? 0 : h[TC_NINT];
-    stats8[2] = s->tree.trivial ? 0 : s->tree.n_cells;
-    stats8[3] = h[TC_GAPS];
-    stats8[4] = h[TC_DEEPER];
-    stats8[5] = h[TC_HASHFAIL];
-    stats8[6] = (int64_t)s->n - h[TC_NIN];
-    stats8[7] = h[TC_OVERFLOW];
-    return NB_OK;
+    try {
+        if (!s || !stats8) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        int rc = ensure_tree(s);
+        if (rc) return rc;
+        int32_t h[TC_COUNT] = {0};
+        cudaError_t e = cudaMemcpy(h, s->tree.counters, sizeof(h), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return tfail(s, NB_ECUDA, cudaGetErrorString(e));
+        stats8[0] = h[TC_NIN];
+        stats8[1] = s->tree.trivial ? 0 : h[TC_NINT];
+        stats8[2] = s->tree.trivial ? 0 : s->tree.n_cells;
+        stats8[3] = h[TC_GAPS];
+        stats8[4] = h[TC_DEEPER];
+        stats8[5] = h[TC_HASHFAIL];
+        stats8[6] = (int64_t)s->n - h[TC_NIN];
+        stats8[7] = h[TC_OVERFLOW];
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 int nb_tree_nodes(nb_sim* s, nb_tree_node* nodes, size_t capacity) {
-    if (!s || (!nodes && capacity)) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    int rc = ensure_tree(s);
-    if (rc) return rc;
-    const TreeBuffers& t = s->tree;
-    if (t.trivial) return NB_OK;
-    const size_t C = (size_t)t.n_cells;
-    if (capacity < C) return tfail(s, NB_EINVAL, "capacity below nb_tree_size");
-    std::vector<float4> com(C), lo(C), hi(C);
-    std::vector<int4> meta(C);
-    std::vector<double> mass(C);
-    std::vector<uint64_t> code(C);
-    std::vector<int32_t> order(s->n), count(C);
-    cudaError_t e = cudaMemcpy(com.data(), t.cell_com, C * 16, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(count.data(), t.cell_count, C * 4, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(lo.data(), t.cell_lo, C * 16, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(hi.data(), t.cell_hi, C * 16, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(meta.data(), t.cell_meta, C * 16, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(mass.data(), t.cell_mass, C * 8, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(code.data(), t.cell_code, C * 8, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(order.data(), t.vals[t.final_buf], s->n * 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return tfail(s, NB_ECUDA, std::string("nb_tree_nodes: ") + cudaGetErrorString(e));
-    for (size_t c = 0; c < C; ++c) {
-        nb_tree_node& o = nodes[c];
-        const int level = (int)hi[c].w;
-        const int kind = meta[c].w & 15;
-        o.level = level;
-        o.count = count[c];
-        o.first_child = kind == TK_INTERNAL ? meta[c].x : -1;
-        o.body = kind == TK_SINGLE ? order[meta[c].x] : -1;
-        o.prefix = level ? (code[c] & ((1ull << (3 * level)) - 1ull)) : 0ull;
-        o.mass = mass[c];
-        o.com[0] = com[c].x; o.com[1] = com[c].y; o.com[2] = com[c].z;
-        o.side = lo[c].w;
-        o.lo[0] = lo[c].x; o.lo[1] = lo[c].y; o.lo[2] = lo[c].z;
-        o.bucket_begin = kind == TK_BUCKET ? meta[c].x : -1;
-        o.bucket_end = kind == TK_BUCKET ? meta[c].x + count[c] : -1;
+    try {
+        if (!s || (!nodes && capacity)) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        int rc = ensure_tree(s);
+        if (rc) return rc;
+        const TreeBuffers& t = s->tree;
+        if (t.trivial) return NB_OK;
+        const size_t C = (size_t)t.n_cells;
+        if (capacity < C) return tfail(s, NB_EINVAL, "capacity below nb_tree_size");
+        std::vector<float4> com(C), lo(C), hi(C);
+        std::vector<int4> meta(C);
+        std::vector<double> mass(C);
+        std::vector<uint64_t> code(C);
+        std::vector<int32_t> order(s->n), count(C);
+        cudaError_t e = cudaMemcpy(com.data(), t.cell_com, C * 16, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(count.data(), t.cell_count, C * 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(lo.data(), t.cell_lo, C * 16, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(hi.data(), t.cell_hi, C * 16, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(meta.data(), t.cell_meta, C * 16, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(mass.data(), t.cell_mass, C * 8, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(code.data(), t.cell_code, C * 8, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(order.data(), t.vals[t.final_buf], s->n * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return tfail(s, NB_ECUDA, std::string("nb_tree_nodes: ") + cudaGetErrorString(e));
+        for (size_t c = 0; c < C; ++c) {
+            nb_tree_node& o = nodes[c];
+            const int level = (int)hi[c].w;
+            const int kind = meta[c].w & 15;
+            o.level = level;
+            o.count = count[c];
+            o.first_child = kind == TK_INTERNAL ? meta[c].x : -1;
+            o.body = kind == TK_SINGLE ? order[meta[c].x] : -1;
+            o.prefix = level ? (code[c] & ((1ull << (3 * level)) - 1ull)) : 0ull;
+            o.mass = mass[c];
+            o.com[0] = com[c].x; o.com[1] = com[c].y; o.com[2] = com[c].z;
+            o.side = lo[c].w;
+            o.lo[0] = lo[c].x; o.lo[1] = lo[c].y; o.lo[2] = lo[c].z;
+            o.bucket_begin = kind == TK_BUCKET ? meta[c].x : -1;
+            o.bucket_end = kind == TK_BUCKET ? meta[c].x + count[c] : -1;
+        }
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
     }
-    return NB_OK;
 }
 
 int nb_tree_order(nb_sim* s, int32_t* order) {
-    if (!s || !order) return NB_EINVAL;
-    cudaSetDevice(s->dev);
-    int rc = ensure_tree(s);
-    if (rc) return rc;
-    cudaError_t e = cudaMemcpy(order, s->tree.vals[s->tree.final_buf], s->n * 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return tfail(s, NB_ECUDA, cudaGetErrorString(e));
-    return NB_OK;
+    try {
+        if (!s || !order) return NB_EINVAL;
+        cudaSetDevice(s->dev);
+        int rc = ensure_tree(s);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpy(order, s->tree.vals[s->tree.final_buf], s->n * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return tfail(s, NB_ECUDA, cudaGetErrorString(e));
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
 }
 
 }  // extern "C"
