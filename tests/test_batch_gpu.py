@@ -184,3 +184,29 @@ def test_batch_without_galaxies_is_refused():
     with pytest.raises(nb.NBodyError):
         b.commit()
     b.close()
+
+
+def test_full_size_config4_error_bounds():
+    """The 512-galaxy batch of the batched workload (n log-uniform in
+    [256, 65,536], Plummer or disk): every Barnes-Hut member within 1e-3 of
+    the FP64 direct sum on sampled bodies, sampled direct members within 1e-5
+    of the plain direct path."""
+    import bench_forms
+    gals = bench_forms.batch_galaxies(nb)
+    with nb.NBodyBatch(bh_threshold=8192, bh_theta=0.6, softening2=EPS2) as b:
+        for pm, v in gals:
+            b.add(pm, v)
+        b.commit()
+        worst = 0.0
+        direct_checked = 0
+        for g, (pm, v) in enumerate(gals):
+            n = pm.shape[0]
+            if n >= 8192:
+                t = np.arange(0, n, max(1, n // 128)).astype(np.int32)
+                err = O.rel_l2(b.forces(g)[t], fp64_forces(pm, v, t))
+                worst = max(worst, err)
+                assert err < BH_FP64_TOL, (g, n, err)
+            elif g % 16 == 0:
+                assert O.rel_l2(b.forces(g), plain_direct_forces(pm, v)) < DIRECT_TOL, (g, n)
+                direct_checked += 1
+        assert direct_checked >= 10

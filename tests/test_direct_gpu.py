@@ -190,3 +190,30 @@ def test_render_vertices_headless():
     np.testing.assert_array_equal(rv["position"], pm[:, :3])
     np.testing.assert_array_equal(rv["colour"], col)
     assert np.all(rv["scale"] == 2.0)
+
+
+def test_full_size_config3_properties():
+    """N = 262,144 (two Plummer spheres on a parabolic orbit, eps = 0.01):
+    forces within 1e-5 of the FP64 direct sum on sampled targets, Newton's third
+    law (net force ~ 0 against the sum of magnitudes) and the energy change of
+    a step within the integrator's own error, properties that need no CPU run
+    of 6.9e10 interactions."""
+    n = 262144
+    pm, v = nb.seed_collision(1234, n)
+    rng = np.random.default_rng(7)
+    targets = np.sort(rng.choice(n, 2048, replace=False)).astype(np.int32)
+    with direct_sim(softening2=1e-4) as s:
+        s.init_soa(pm, v)
+        F = s.compute_forces()
+        F64 = s.fp64_forces(targets)
+        assert O.rel_l2(F[targets], F64) < FORCE_TOL
+        net = np.abs(F.sum(axis=0)).max()          # F is the force m * a on each body
+        scale = np.linalg.norm(F, axis=1).sum()
+        assert net < 1e-6 * scale, (net, scale)
+        # the reference's kick-drift (symplectic Euler) changes the energy by
+        # O(dt) per step: 1.05e-5 of it here at dt = 1e-3; a broken force or
+        # update would be off by orders of magnitude
+        e0 = s.diagnostics(0.0)["total"]
+        s.step(1e-3, 1)
+        e1 = s.diagnostics(0.5e-3)["total"]
+        assert abs(e1 - e0) < 1e-4 * abs(e0), (e0, e1)
