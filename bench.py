@@ -30,7 +30,7 @@ against the FP64 direct sum); --no-forms leaves them out.
 --impl reference times the reference's CPU algorithm (the oracle's
 restatement of BruteForceCPU / BarnesHut on all host cores) on the same
 workload, a bounded sample per step.
-Multi-GPU: the step does not shard across GPUs in this build; --gpus N runs N
+Multi-GPU: the step does not shard across GPUs; --gpus N runs N
 independent replicas (one galaxy per rank, different seeds) and reports the
 aggregate.
 """

@@ -1,6 +1,6 @@
 // nb_fp64.cu -- FP64 direct-sum oracle (K8) and FP64 diagnostics.
 //
-// The FP64 oracle is the judge of force error: for m sampled target bodies it
+// The FP64 oracle measures force error: for m sampled target bodies it
 // sums the exact force law in double precision over all n sources, from the
 // same float positions and masses the FP32 kernels use.  The diagnostics
 // reduce kinetic energy, linear and angular momentum, mass and centre of mass
