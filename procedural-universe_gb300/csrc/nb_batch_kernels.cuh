@@ -193,6 +193,9 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
         record_error(err, DEV_TREE_OVERFLOW);
         return;
     }
+    // children sit one level below their node (a node exists at every level
+    // where two or more bodies still share the key prefix)
+    const int level = (int)__ldcg(&cell_hi[c]).w;
     float4 ccm[8], cq1[8], cq2[8];
     float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     int count = 0;
@@ -216,8 +219,7 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
             ccm[j] = __ldcg(&cell_com[ch]);
             cq1[j] = cq2[j] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        if (kind != BK_INTERNAL)
-            __stcg(&cell_walk[ch], walk_record(mt.x, cnt, mt.x, kind, 0, (int)__ldcg(&cell_hi[ch]).w));
+        if (kind != BK_INTERNAL) __stcg(&cell_walk[ch], walk_record(mt.x, cnt, mt.x, kind, 0, level + 1));
         m += ccm[j].w;
         cx = fmaf(ccm[j].w, ccm[j].x, cx); cy = fmaf(ccm[j].w, ccm[j].y, cy); cz = fmaf(ccm[j].w, ccm[j].z, cz);
         count += cnt;
@@ -239,7 +241,7 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
     __stcg(&cell_q1[c], make_float4(xx, yy, zz, 0.f));
     __stcg(&cell_q2[c], make_float4(xy, xz, yz, 0.f));
     __stcg(&cell_count[c], count);
-    __stcg(&cell_walk[c], walk_record(F, count, int_first[k], BK_INTERNAL, nch, (int)__ldcg(&cell_hi[c]).w));
+    __stcg(&cell_walk[c], walk_record(F, count, int_first[k], BK_INTERNAL, nch, level));
 }
 
 __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_dev,
