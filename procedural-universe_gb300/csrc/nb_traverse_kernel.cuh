@@ -89,7 +89,10 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                                                          float4* __restrict__ acc,
                                                          unsigned long long* __restrict__ inter,
                                                          int* __restrict__ err) {
-    __shared__ int4 stk[kTravWarps][kStack];   // (child range, lanes of body slot 0, of slot 1, 0)
+    // 12-byte entries (child range, lanes of body slot 0, of slot 1): the smaller the
+    // shared-memory footprint, the more of the SM's L1 is left for the node reads
+    struct StackEntry { int range, lanes0, lanes1; };
+    __shared__ StackEntry stk[kTravWarps][kStack];
     __shared__ float4 kid_cm[kTravWarps][32];
     __shared__ int4 kid_mt[kTravWarps][32];
     __shared__ float4 lc_src[kTravWarps][kListCells];
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                 const unsigned cf = (unsigned)cmt.x, cn = ((unsigned)cmt.w >> 4) & 15u;
                 ok = cf < (1u << kRangeBits) && cn >= 1 && cn <= 8 && cf + cn <= (unsigned)n_cells;
                 if (ok && top + __popc(bO) <= kStack)
-                    stk[w][top + __popc(bO & lt)] = make_int4((int)(cf | (cn << kRangeBits)), (int)cm0, (int)cm1, 0);
+                    stk[w][top + __popc(bO & lt)] = StackEntry{(int)(cf | (cn << kRangeBits)), (int)cm0, (int)cm1};
             }
             if (!__all_sync(0xffffffffu, ok) || top + __popc(bO) > kStack) bad = true;
             top += __popc(bO);
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
                 const int4 mt = kid_mt[w][j];
                 const unsigned cf = (unsigned)mt.x, cn = ((unsigned)mt.w >> 4) & 15u;
                 if (top < kStack && cf < (1u << kRangeBits) && cn >= 1 && cn <= 8 && cf + cn <= (unsigned)n_cells) {
-                    if (lane == 0) stk[w][top] = make_int4((int)(cf | (cn << kRangeBits)), (int)b0, (int)b1, 0);
+                    if (lane == 0) stk[w][top] = StackEntry{(int)(cf | (cn << kRangeBits)), (int)b0, (int)b1};
                     ++top;
                 } else {
                     bad = true;
@@ -343,11 +346,11 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const float4* __restric
         unsigned eF = 0, em0 = 0, em1 = 0;
         int en = 0;
         if (lane < cap && lane < top) {
-            const int4 e = stk[w][top - 1 - lane];
-            eF = (unsigned)e.x & ((1u << kRangeBits) - 1u);
-            en = (int)((unsigned)e.x >> kRangeBits);
-            em0 = (unsigned)e.y;
-            em1 = (unsigned)e.z;
+            const StackEntry e = stk[w][top - 1 - lane];
+            eF = (unsigned)e.range & ((1u << kRangeBits) - 1u);
+            en = (int)((unsigned)e.range >> kRangeBits);
+            em0 = (unsigned)e.lanes0;
+            em1 = (unsigned)e.lanes1;
         }
         int incl = en;   // inclusive prefix of the child counts over lanes 0..7
         for (int o = 1; o < 8; o <<= 1) {
