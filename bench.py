@@ -436,7 +436,7 @@ def run_forms(args):
                                                 ("value", "theta", "force_rel_l2_vs_fp64_largest")},
             "speedup_vs_sequential_plain_equal_accuracy": r["speedup_vs_sequential_plain_equal_accuracy"],
         }
-        for k in ("latency_s", "e2e", "tuning", "makespan_s", "server_timing", "served_equal_accuracy"):
+        for k in ("latency_s", "e2e", "tuning", "makespan_s", "server_timing", "served_equal_accuracy", "gpu_launches"):
             if r.get(k) is not None:
                 out[name][k] = r[k]
     out["served"]["sequential_plain_equal_accuracy"]["latency_s"] = \

@@ -283,6 +283,7 @@ def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, t
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
         "makespan_s": makespan, "rounds": rounds, "server_timing": timing,
+        "gpu_launches": timing["step_launches"],
         "force_rel_l2_vs_fp64_largest": served_err,
         "sequential_plain": {"value": seq_value, "unit": METRIC, "theta": theta,
                              "force_rel_l2_vs_fp64_largest": plain_err,
@@ -322,6 +323,7 @@ def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]
         torch.cuda.synchronize()
+        l0 = b.launch_count()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
                 flush.zero_()
@@ -331,6 +333,7 @@ def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
         torch.cuda.synchronize()
         t = float(sum(a.elapsed_time(c) for a, c in evs)) / args.steps
         inf, st = b.info(), b.tree_stats()
+        inf["launches"] = b.launch_count() - l0
         b.close()
         return t, e, inf, st
 
@@ -354,6 +357,7 @@ def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
         "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxy)",
         "config": {"workload": "bh1m_batched", "n": n, "theta": theta, "eps": eps, "dt": dt,
                    "l2": "flushed (512 MB write) before every timed step"},
+        "gpu_launches": info["launches"],
         "force_rel_l2_vs_fp64": err, "interactions_per_body": info["interactions"] / n,
         "groups": stats["groups"], "bodies_per_group": n / max(1, stats["groups"]),
         "plain": {"value": plain, "theta": theta, "force_rel_l2_vs_fp64": plain_err},
@@ -381,11 +385,13 @@ def run_batch(args, nb, torch):
     b.step(dt, args.warmup)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
+    launches0 = b.launch_count()
     for k in range(args.steps):
         evs[k][0].record(stream)
         b.step(dt, 1)
         evs[k][1].record(stream)
     torch.cuda.synchronize()
+    gpu_launches = b.launch_count() - launches0
     ms = float(sum(a.elapsed_time(c) for a, c in evs))
     value = n_real * args.steps / (ms * 1e-3)
     info = b.info()
@@ -429,7 +435,7 @@ def run_batch(args, nb, torch):
     return {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies)",
+        "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies)", "gpu_launches": gpu_launches,
         "config": {"workload": "batch512", "galaxies": len(gals), "bodies": n_real,
                    "barnes_hut_members": len(bh_ids), "theta": theta, "eps": 0.01, "dt": dt,
                    "l2": "inputs (%.0f MB of state) larger than L2" % (n_real * 64 / 1e6)},

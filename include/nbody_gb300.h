@@ -288,6 +288,8 @@ int  nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4);
 /* Forces (n x 3 doubles) of one galaxy at the current state. */
 int  nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3);
 int  nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last);
+/* Kernel launches of this batch so far (each graph replay counts its kernels). */
+int  nb_batch_launch_count(nb_batch* b, uint64_t* launches);
 /* Forest of the last step: stats4 = {traversal groups, internal nodes, cells,
  * Barnes-Hut bodies}. */
 int  nb_batch_tree_stats(nb_batch* b, int64_t* stats4);
@@ -352,10 +354,11 @@ int  nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, 
 /* Body-steps completed and rounds run since creation. */
 int  nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds);
 /* Where the server's time went: batch rebuilds (count, seconds: new batch,
- * hand-over, upload, tree sizing), stepping (seconds, steps of the batch), and
- * host generation of initial conditions (seconds). Any pointer may be NULL. */
+ * hand-over, upload, tree sizing), stepping (seconds, steps of the batch, kernel
+ * launches of those steps), and host generation of initial conditions
+ * (seconds). Any pointer may be NULL. */
 int  nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
-                      double* generate_s);
+                      double* generate_s, uint64_t* step_launches);
 
 /* ---- allocation-free direct sum -------------------------------------------- */
 /* No counterpart in the reference.  For callers that must not allocate device

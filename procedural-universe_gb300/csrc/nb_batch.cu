@@ -665,6 +665,16 @@ int nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3) {
     }
 }
 
+int nb_batch_launch_count(nb_batch* b, uint64_t* launches) {
+    try {
+        if (!b || !launches) return NB_EINVAL;
+        *launches = b->core ? b->core->prof.launches : 0;
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
+}
+
 int nb_batch_info(nb_batch* b, size_t* galaxies, size_t* bodies, uint64_t* interactions_last) {
     try {
         if (!b) return NB_EINVAL;

@@ -61,7 +61,7 @@ struct nb_server {
     float dt = NAN;                 // dt of the active jobs
     double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
-    uint64_t rebuilds = 0, batch_steps = 0;           // where the time went
+    uint64_t rebuilds = 0, batch_steps = 0, step_launches = 0;   // where the time went
     double rebuild_s = 0, stepping_s = 0, generate_s = 0;
 };
 
@@ -278,7 +278,11 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
             }
             k = std::max(k, 1);
             const double t_round = now_s(s);
+            uint64_t l0 = 0, l1 = 0;
+            nb_batch_launch_count(s->batch, &l0);
             int rc = batch_launch_steps(s->batch, s->dt, k);
+            nb_batch_launch_count(s->batch, &l1);
+            s->step_launches += l1 - l0;
             if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
             // meanwhile: initial conditions of the queued jobs the next admission can take
             bool generated = false;
@@ -350,7 +354,7 @@ int nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, s
 }
 
 int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
-                     double* generate_s) {
+                     double* generate_s, uint64_t* step_launches) {
     try {
         if (!s) return NB_EINVAL;
         if (rebuilds) *rebuilds = s->rebuilds;
@@ -358,6 +362,7 @@ int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64
         if (batch_steps) *batch_steps = s->batch_steps;
         if (step_s) *step_s = s->stepping_s;
         if (generate_s) *generate_s = s->generate_s;
+        if (step_launches) *step_launches = s->step_launches;
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed
         return NB_ENOMEM;

@@ -438,6 +438,7 @@ def _bind_batch():
         "nb_batch_read": ([vp, i32, vp, vp], i32),
         "nb_batch_forces": ([vp, i32, vp], i32),
         "nb_batch_info": ([vp, vp, vp, vp], i32),
+        "nb_batch_launch_count": ([vp, vp], i32),
         "nb_batch_tree_stats": ([vp, vp], i32),
         "nb_batch_stream": ([vp], vp),
         "nb_batch_write_state": ([vp, vp, vp], i32),
@@ -549,6 +550,11 @@ class NBodyBatch:
         self._check(lib().nb_batch_info(self._h, ctypes.byref(ng), ctypes.byref(nb_), ctypes.byref(it)),
                     "nb_batch_info")
         return dict(galaxies=ng.value, bodies=nb_.value, interactions=it.value)
+
+    def launch_count(self) -> int:
+        v = ctypes.c_uint64(0)
+        self._check(lib().nb_batch_launch_count(self._h, ctypes.byref(v)), "nb_batch_launch_count")
+        return int(v.value)
 
     def tree_stats(self):
         s = (ctypes.c_int64 * 4)()

@@ -40,7 +40,7 @@ def _bind():
         "nb_server_status": ([vp, ctypes.c_uint64, vp], i32),
         "nb_server_result": ([vp, ctypes.c_uint64, vp, vp, sz], i32),
         "nb_server_stats": ([vp, vp, vp], i32),
-        "nb_server_timing": ([vp, vp, vp, vp, vp, vp], i32),
+        "nb_server_timing": ([vp, vp, vp, vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -133,9 +133,10 @@ class NBodyServer:
 
     def timing(self):
         """Rebuilds (count, seconds), batch steps (count, seconds) and host generation seconds."""
-        nr, ns_ = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        nr, ns_, nl = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
         rs, ss, gs = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
         self._check(nb.lib().nb_server_timing(self._h, ctypes.byref(nr), ctypes.byref(rs), ctypes.byref(ns_),
-                                              ctypes.byref(ss), ctypes.byref(gs)), "nb_server_timing")
+                                              ctypes.byref(ss), ctypes.byref(gs), ctypes.byref(nl)),
+                    "nb_server_timing")
         return dict(rebuilds=nr.value, rebuild_s=rs.value, batch_steps=ns_.value, step_s=ss.value,
-                    generate_s=gs.value)
+                    generate_s=gs.value, step_launches=nl.value)
