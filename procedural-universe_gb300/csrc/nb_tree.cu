@@ -715,6 +715,9 @@ static cudaError_t launch_keys(nb_sim* sim, size_t nk) {
     return cudaGetLastError();
 }
 
+__global__ void k_sort_finalize(uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1, int32_t* __restrict__ v0,
+                                const int32_t* __restrict__ v1, int n, const int32_t* __restrict__ plan);
+
 cudaError_t tree_build(nb_sim* sim) {
     TreeBuffers& t = sim->tree;
     const int n = (int)sim->n;
@@ -737,14 +740,14 @@ cudaError_t tree_build(nb_sim* sim) {
         }
         NB_TRY(cudaGetLastError());
     }
-    // The sort result's buffer is decided on the device; read the plan with the counters below.
+    // The sort result's buffer is decided on the device (passes with a constant
+    // digit are skipped): a copy on the device brings it to buffer 0 when it
+    // ended in buffer 1, so no host read is needed here.
     {
-        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 3);
-        // Gather needs the final buffer: run it for both candidates' source after reading the plan.
-        NB_TRY(cudaMemcpyAsync(t.h_counters + 7, t.plan + 16, 4, cudaMemcpyDeviceToHost, st));
-        NB_TRY(cudaStreamSynchronize(st));
-        t.final_buf = t.h_counters[7];
-        k_gather<<<(n + 255) / 256, 256, 0, st>>>(sim->pos, t.vals[t.final_buf], n, t.spos);
+        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 4);
+        k_sort_finalize<<<(n + 255) / 256, 256, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], n, t.plan);
+        t.final_buf = 0;
+        k_gather<<<(n + 255) / 256, 256, 0, st>>>(sim->pos, t.vals[0], n, t.spos);
         TopoView tv = topo_view(sim);
         k_positions<<<(n + 255) / 256, 256, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters);
         NB_TRY(exclusive_scan(t.pos_nint, t.pos_nint, n, t.scan_sums, t.counters + TC_NINT, st));
