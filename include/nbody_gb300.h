@@ -351,6 +351,10 @@ double nb_server_clock(nb_server* s);
 int  nb_server_status(nb_server* s, uint64_t id, nb_job_status* out);
 /* Copies a finished job's final state (n x float4 each) to the host. */
 int  nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, size_t n);
+/* Forgets a finished (or rejected) job and frees its host copy of the result;
+ * a serving loop calls it once the result has been taken, so that the server's
+ * memory does not grow with the number of jobs served. */
+int  nb_server_release(nb_server* s, uint64_t id);
 /* Body-steps completed and rounds run since creation. */
 int  nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds);
 /* Where the server's time went: batch rebuilds (count, seconds: new batch,

@@ -353,6 +353,20 @@ int nb_server_result(nb_server* s, uint64_t id, float* pos_mass4, float* vel4, s
     }
 }
 
+int nb_server_release(nb_server* s, uint64_t id) {
+    try {
+        if (!s) return NB_EINVAL;
+        auto it = s->jobs.find(id);
+        if (it == s->jobs.end()) return sfail(s, NB_EINVAL, "unknown job");
+        if (it->second.st.state != 2 && it->second.st.state != -1)
+            return sfail(s, NB_EBADSTATE, "only a finished or rejected job can be released");
+        s->jobs.erase(it);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
+}
+
 int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
                      double* generate_s, uint64_t* step_launches) {
     try {

@@ -39,6 +39,7 @@ def _bind():
         "nb_server_clock": ([vp], ctypes.c_double),
         "nb_server_status": ([vp, ctypes.c_uint64, vp], i32),
         "nb_server_result": ([vp, ctypes.c_uint64, vp, vp, sz], i32),
+        "nb_server_release": ([vp, ctypes.c_uint64], i32),
         "nb_server_stats": ([vp, vp, vp], i32),
         "nb_server_timing": ([vp, vp, vp, vp, vp, vp, vp], i32),
     }
@@ -125,6 +126,11 @@ class NBodyServer:
         v = np.zeros((n, 4), np.float32)
         self._check(nb.lib().nb_server_result(self._h, jid, nb._ptr(pm), nb._ptr(v), n), "nb_server_result")
         return pm, v
+
+    def release(self, jid):
+        """Forgets a finished or rejected job (frees its result)."""
+        self._check(nb.lib().nb_server_release(self._h, jid), "nb_server_release")
+        self.n_of.pop(jid, None)
 
     def stats(self):
         bs, r = ctypes.c_uint64(0), ctypes.c_uint64(0)

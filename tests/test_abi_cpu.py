@@ -156,3 +156,20 @@ def test_server_rejects_jobs_that_can_never_fit():
     with ns.NBodyServer() as s:   # 120 GB budget: 110 M bodies fit it, not one batch's octree
         too_many = s.submit(3, 110 << 20, 10, 1e-3, 0)
         assert s.status(too_many)["state"] == -1
+
+
+def test_server_release_of_rejected_and_unknown_jobs():
+    """A rejected job can be released (it never reaches the device); a queued
+    job cannot; an unknown id is an error."""
+    import nbody_gb300 as nb
+    import nbody_serve as ns
+    with ns.NBodyServer(memory_budget=640 * 10_000) as s:
+        queued = s.submit(1, 5_000, 10, 1e-3, 0)
+        rejected = s.submit(2, 20_000, 10, 1e-3, 0)
+        s.release(rejected)
+        with pytest.raises(nb.NBodyError):
+            s.status(rejected)
+        with pytest.raises(nb.NBodyError):
+            s.release(queued)
+        with pytest.raises(nb.NBodyError):
+            s.release(12345)

@@ -67,6 +67,9 @@ def test_result_matches_batched_form():
     with ns.NBodyServer(max_active=4, steps_per_round=4, bh_threshold=8192) as s:
         (i,), _ = run_all(s, [(seed, n, model)], 12)
         pr, vr = s.result(i)
+        s.release(i)                        # the result is taken: the server forgets the job
+        with pytest.raises(nb.NBodyError):
+            s.status(i)
     pm, v = nb.seed_disk(seed, n)
     with nb.NBodyBatch(bh_threshold=8192, bh_theta=0.5, softening2=0.005 ** 2) as b:
         b.add(pm, v)
