@@ -200,3 +200,51 @@ def test_full_size_config2_keys_topology_and_force_error():
     Fo = t.forces_subset(targets, G=1.0, S=0.005 ** 2, theta=0.5)
     assert O.rel_l2(F[targets], Fo) < 1e-5
     assert O.rel_l2(F[targets], F64) < REF_ALGO_FP64_TOL
+
+
+def test_reinit_same_count_new_tree_shape():
+    """Re-initialising a simulator with the same body count but a tree of a
+    different shape (many more internal nodes than the node arrays were sized
+    for; then no body inside the root cube; then the first set again) steps to
+    exactly what a fresh simulator computes: node arrays grow, and no node of
+    an earlier tree leaks into the next."""
+    rng = np.random.default_rng(21)
+    n = 16384
+    S = 1e-4
+
+    def state(pos):
+        pm = np.zeros((n, 4), np.float32)
+        pm[:, :3] = pos
+        pm[:, 3] = 1.0 / n
+        v = np.zeros((n, 4), np.float32)
+        v[:, :3] = rng.normal(scale=1e-3, size=(n, 3))
+        return nb.records_from_soa(pm, v)
+
+    uniform = state(rng.uniform(-1, 1, (n, 3)))
+    centres = rng.uniform(-1, 1, (n // 2, 3))
+    pairs = state(np.concatenate([centres, centres + 1e-4]))   # deep chains: many more internal nodes
+    outside = state(rng.uniform(1e5, 2e5, (n, 3)))              # no body in the root cube
+    dt = 1e-3
+
+    def fresh(rec, k):
+        with bh_sim(theta=0.5, softening2=S) as f:
+            f.init(rec)
+            f.step(dt, k)
+            out = rec.copy()
+            f.write_back(out)
+        return out
+
+    with bh_sim(theta=0.5, softening2=S) as s:
+        s.init(uniform)
+        s.step(dt, 2)
+        small = s.tree_stats()
+        for rec, k in ((pairs, 2), (outside, 1), (uniform, 2)):
+            s.init(rec)
+            s.step(dt, k)
+            out = rec.copy()
+            s.write_back(out)
+            ref = fresh(rec, k)
+            for f in ("position", "velocity", "forces"):
+                assert np.array_equal(out[f], ref[f]), f
+            if rec is pairs:
+                assert s.tree_stats()["internal"] > 2 * small["internal"]
