@@ -267,7 +267,8 @@ typedef struct nb_tuning {
 int  nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta, nb_batch** out);
 int  nb_batch_destroy(nb_batch* b);
 const char* nb_batch_last_error(const nb_batch* b);
-/* Adds one galaxy (host buffers n x float4 each); galaxy receives its index. */
+/* Adds one galaxy (host buffers n x float4 each, 1 <= n <= 16 Mi = 16,777,216);
+ * galaxy receives its index. */
 int  nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t n, int32_t* galaxy);
 /* Uploads every galaxy, lays out the tables and sizes the tree buffers. */
 int  nb_batch_commit(nb_batch* b);
@@ -304,7 +305,7 @@ void* nb_batch_stream(nb_batch* b);
  * bytes of the active jobs (640 bytes per body: state, sort and topology
  * scratch, tree cells with quadrupoles at twice their measured count)
  * stay within memory_budget, their bodies within 96 Mi (the batched octree's
- * cell-index range; a larger job is rejected) and a slot is free, and are stepped together in
+ * cell-index range) and a slot is free, and are stepped together in
  * rounds by the batched form; a round takes at most steps_per_round steps,
  * never more than the nearest job completion and, with round_seconds > 0
  * (default 0.1), no more than fit in round_seconds at the batch's measured
@@ -341,7 +342,10 @@ int  nb_server_default_params(nb_server_params* p);
 int  nb_server_create(const nb_server_params* p, nb_server** out);
 int  nb_server_destroy(nb_server* s);
 const char* nb_server_last_error(const nb_server* s);
-/* Queues a job; its initial conditions are generated when it is admitted. */
+/* Queues a job; its initial conditions are generated when it is admitted.  A job
+ * of more than 16 Mi bodies (the batched form's galaxy limit) or of more
+ * estimated bytes than memory_budget can never run: it is recorded with
+ * state -1 (rejected) and the call returns NB_OK. */
 int  nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id);
 /* One scheduling round: retire finished jobs (final state kept on the host),
  * admit queued jobs that fit the budget and the free slots, step the active

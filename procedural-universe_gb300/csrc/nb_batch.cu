@@ -350,6 +350,7 @@ int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const f
                      size_t n, int32_t* galaxy) {
     if (!b || !pos || !posc || !vel || !velc || n == 0) return NB_EINVAL;
     if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
+    if (n > kMaxGalaxyBodies) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
     b->h_pos.emplace_back();
     b->h_vel.emplace_back();
     nb_batch::Gal g;
@@ -460,7 +461,7 @@ int nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t 
     try {
         if (!b || !pos_mass4 || !vel4 || n == 0) return NB_EINVAL;
         if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
-        if (n > (1u << 24)) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
+        if (n > kMaxGalaxyBodies) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
         b->h_pos.emplace_back(pos_mass4, pos_mass4 + 4 * n);
         b->h_vel.emplace_back(vel4, vel4 + 4 * n);
         nb_batch::Gal g;

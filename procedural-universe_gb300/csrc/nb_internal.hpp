@@ -202,6 +202,7 @@ int sim_reserve_zeroed(nb_sim* s, size_t n);
 int sim_check_state(nb_sim* s);
 
 // ---- batched form hand-over (nb_batch.cu), used by the served form ----
+constexpr size_t kMaxGalaxyBodies = (size_t)1 << 24;   // bodies of one galaxy in the batched form
 int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
                      size_t n, int32_t* galaxy);
 int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,

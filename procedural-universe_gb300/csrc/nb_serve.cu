@@ -58,6 +58,7 @@ struct nb_server {
     nb_batch* batch = nullptr;
     size_t bytes_used = 0;
     size_t bodies_used = 0;
+    bool batch_stale = false;       // the active set changed since the batch was built
     float dt = NAN;                 // dt of the active jobs
     double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
@@ -92,13 +93,15 @@ int generate(Job& j) {
 }
 
 // Builds a batch of the active jobs; continuing jobs take their state from
-// the previous batch (device to device).
+// the previous batch (device to device).  On failure the previous batch and
+// the jobs' places in it are left as they were.
 int rebuild(nb_server* s) {
     nb_batch* nb2 = nullptr;
     int rc = nb_batch_create(&s->prm.base, s->prm.bh_threshold, s->prm.base.theta, &nb2);
     if (rc) return sfail(s, rc, "nb_batch_create failed");
-    for (uint64_t id : s->active) {
-        Job& j = s->jobs[id];
+    std::vector<int32_t> place(s->active.size(), -1);
+    for (size_t a = 0; a < s->active.size(); ++a) {
+        const Job& j = s->jobs[s->active[a]];
         int32_t g = -1;
         if (j.galaxy >= 0 && s->batch) {
             const float4 *p, *pc, *v, *vc;
@@ -113,7 +116,7 @@ int rebuild(nb_server* s) {
             nb_batch_destroy(nb2);
             return sfail(s, rc, "batch add: " + m);
         }
-        j.galaxy = g;
+        place[a] = g;
     }
     rc = nb_batch_commit(nb2);
     if (rc) {
@@ -124,8 +127,9 @@ int rebuild(nb_server* s) {
     if (s->batch) nb_batch_destroy(s->batch);
     s->batch = nb2;
     s->step_s = 0;
-    for (uint64_t id : s->active) {
-        Job& j = s->jobs[id];
+    for (size_t a = 0; a < s->active.size(); ++a) {
+        Job& j = s->jobs[s->active[a]];
+        j.galaxy = place[a];
         j.init_pos.clear();
         j.init_pos.shrink_to_fit();
         j.init_vel.clear();
@@ -201,7 +205,7 @@ int nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id) {
         j.st.state = 0;
         j.st.submit_s = now_s(s);
         j.st.bytes = job_bytes(*job);
-        if (j.st.bytes > s->prm.memory_budget || job->n > kMaxBatchBodies) j.st.state = -1;   // can never fit
+        if (job->n > kMaxGalaxyBodies || j.st.bytes > s->prm.memory_budget) j.st.state = -1;   // can never fit
         const uint64_t jid = j.st.id;
         const bool queued = j.st.state == 0;
         s->jobs.emplace(jid, std::move(j));
@@ -216,27 +220,32 @@ int nb_server_submit(nb_server* s, const nb_job* job, uint64_t* id) {
 int nb_server_tick(nb_server* s, int* active, int* queued) {
     try {
         if (!s) return NB_EINVAL;
-        bool changed = false;
-        // retire finished jobs
+        // retire finished jobs (a job whose result cannot be read stays active)
         std::vector<uint64_t> keep;
+        int read_rc = NB_OK;
         for (uint64_t id : s->active) {
             Job& j = s->jobs[id];
-            if (j.st.steps_done >= j.spec.steps) {
+            if (read_rc == NB_OK && j.st.steps_done >= j.spec.steps) {
                 j.res_pos.assign(4 * j.spec.n, 0.f);
                 j.res_vel.assign(4 * j.spec.n, 0.f);
-                int rc = nb_batch_read(s->batch, j.galaxy, j.res_pos.data(), j.res_vel.data());
-                if (rc) return sfail(s, rc, std::string("read result: ") + nb_batch_last_error(s->batch));
+                read_rc = nb_batch_read(s->batch, j.galaxy, j.res_pos.data(), j.res_vel.data());
+                if (read_rc) {
+                    sfail(s, read_rc, std::string("read result: ") + nb_batch_last_error(s->batch));
+                    keep.push_back(id);
+                    continue;
+                }
                 j.st.state = 2;
                 j.st.done_s = now_s(s);
                 j.galaxy = -1;
                 s->bytes_used -= j.st.bytes;
                 s->bodies_used -= j.spec.n;
-                changed = true;
+                s->batch_stale = true;
             } else {
                 keep.push_back(id);
             }
         }
         s->active.swap(keep);
+        if (read_rc) return read_rc;
         if (s->active.empty()) s->dt = NAN;
         // admit queued jobs (FIFO) while a slot and the budget allow
         while (!s->queue.empty() && (int)s->active.size() < s->prm.max_active) {
@@ -256,17 +265,21 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
             s->dt = j.spec.dt;
             s->active.push_back(j.st.id);
             s->queue.pop_front();
-            changed = true;
+            s->batch_stale = true;
         }
-        if (changed && !s->active.empty()) {
+        // a rebuild that failed is tried again on the next tick: no round runs
+        // on a batch that does not hold exactly the active jobs
+        if (s->batch_stale && !s->active.empty()) {
             const double t_rb = now_s(s);
             int rc = rebuild(s);
             if (rc) return rc;
             s->rebuild_s += now_s(s) - t_rb;
             ++s->rebuilds;
-        } else if (s->active.empty() && s->batch) {
-            nb_batch_destroy(s->batch);
+            s->batch_stale = false;
+        } else if (s->active.empty()) {
+            if (s->batch) nb_batch_destroy(s->batch);
             s->batch = nullptr;
+            s->batch_stale = false;
         }
         // one round
         if (!s->active.empty()) {

@@ -145,8 +145,8 @@ def test_seeders_match_golden_inputs():
 
 def test_server_rejects_jobs_that_can_never_fit():
     """Admission bounds checked at submission, before any device work: a job
-    larger than the memory budget or than one batch's octree can index is
-    rejected (state -1) and never queued."""
+    larger than the memory budget or than the batched form's galaxy limit
+    (16 Mi bodies) is rejected (state -1) and never queued."""
     import nbody_serve as ns
     with ns.NBodyServer(memory_budget=640 * 10_000) as s:
         small = s.submit(1, 5_000, 10, 1e-3, 0)
@@ -156,6 +156,10 @@ def test_server_rejects_jobs_that_can_never_fit():
     with ns.NBodyServer() as s:   # 120 GB budget: 110 M bodies fit it, not one batch's octree
         too_many = s.submit(3, 110 << 20, 10, 1e-3, 0)
         assert s.status(too_many)["state"] == -1
+        largest = s.submit(4, 16 << 20, 10, 1e-3, 0)        # one galaxy's limit: queued
+        over_galaxy = s.submit(5, (16 << 20) + 1, 10, 1e-3, 0)
+        assert s.status(largest)["state"] == 0
+        assert s.status(over_galaxy)["state"] == -1
 
 
 def test_server_release_of_rejected_and_unknown_jobs():
