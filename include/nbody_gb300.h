@@ -283,7 +283,10 @@ int  nb_batch_get_tuning(nb_batch* b, nb_tuning* t);
  * tilings, for trial_steps graph replays each (state restored after each
  * trial) and keeps the fastest. */
 int  nb_batch_autotune(nb_batch* b, float dt, int trial_steps);
-/* nsteps kick-drift steps of every galaxy, replayed from a captured CUDA graph. */
+/* nsteps kick-drift steps of every galaxy, replayed from a captured CUDA graph.
+ * The octree's arrays are sized at commit to twice the counts then; steps whose
+ * tree outgrows them leave the state unchanged on the device, and the call sizes
+ * the tree from the current state and runs those steps again before it returns. */
 int  nb_batch_step(nb_batch* b, float dt, int nsteps);
 int  nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4);
 /* Forces (n x 3 doubles) of one galaxy at the current state. */
@@ -295,7 +298,8 @@ int  nb_batch_launch_count(nb_batch* b, uint64_t* launches);
  * Barnes-Hut bodies}. */
 int  nb_batch_tree_stats(nb_batch* b, int64_t* stats4);
 /* Whole-batch state transfer, galaxies in index order concatenated (the sum
- * of their n bodies x float4): upload from / download to host buffers. */
+ * of their n bodies x float4): upload from / download to host buffers.  A
+ * written state may need a larger octree; the next step sizes it. */
 int  nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4);
 int  nb_batch_read_state(nb_batch* b, float* pos_mass4, float* vel4);
 void* nb_batch_stream(nb_batch* b);

@@ -66,6 +66,10 @@ struct nb_batch {
     size_t part_cap = 0;
     int* next_unit = nullptr;
     uint64_t direct_pairs = 0;
+    // steps whose octree did not fit its arrays leave the state unchanged and
+    // count here; the wait resizes the tree and runs them again
+    int* held = nullptr;
+    float pending_dt = 0.f;
     // tuning and graph
     nb_tuning tune{128, 1, 1024, 16, 128};
     cudaGraphExec_t exec = nullptr;
@@ -185,16 +189,15 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
             PhaseScope ps(c, NB_PHASE_MASS, 3);
             NB_BCUDA(b, cudaMemsetAsync(t.int_pending, 0, t.int_cap * 4, st));
             k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
-                (int)t.int_cap, t.counters + TC_NINT, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
+                (int)t.int_cap, t.counters, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
                 t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_walk,
                 t.cell_meta, t.cell_hi, (int)t.cell_cap, n, c->d_err);
             k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
-                                                                 t.int_cell, t.counters + TC_NINT, (int)t.int_cap,
-                                                                 b->gal_root,
-                                                                 c->d_err);
+                                                                 t.int_cell, t.counters, (int)t.int_cap,
+                                                                 (int)t.cell_cap, b->gal_root, c->d_err);
             NB_BCUDA(b, cudaMemsetAsync(b->group_ctr, 0, 2 * sizeof(int), st));
             k_batch_groups<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
-                (int)t.int_cap, t.counters + TC_NINT, t.int_cell, b->cell_walk,
+                (int)t.int_cap, t.counters, t.int_cell, b->cell_walk,
                 t.vals[0], b->body_slot, (int)t.cell_cap, n, b->groups, b->group_cap, b->group_ctr, c->d_err);
         }
         {
@@ -236,7 +239,7 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
         NB_BCUDA(b, cudaGetLastError());
     }
     if (update) {
-        NB_BCUDA(b, kick_drift(c, dt));
+        NB_BCUDA(b, kick_drift(c, dt, b->n_bh > 0 ? t.counters : nullptr, (int)t.int_cap, (int)t.cell_cap, b->held));
     }
     return NB_OK;
 }
@@ -320,15 +323,27 @@ int build_graph(nb_batch* b, float dt) {
     return NB_OK;
 }
 
-int sync_check(nb_batch* b) {
+// Host side of tree_fits: the counts of the last build against the capacities.
+bool tree_counts_fit(const nb_batch* b, const int32_t* h) {
+    const TreeBuffers& t = b->core->tree;
+    return h[TC_OVERFLOW] == 0 && h[TC_HASHFAIL] == 0 && (size_t)h[TC_NINT] <= t.int_cap &&
+           (size_t)h[TC_NINT] + (size_t)h[TC_NLEAF] <= t.cell_cap;
+}
+
+// Waits for the stream; *fits (if given) receives whether the last octree
+// fitted its arrays, otherwise a tree that did not is an error.
+int sync_check(nb_batch* b, bool* fits = nullptr) {
     int rc = nb_synchronize(b->core);
     if (rc) return bfail(b, rc, nb_last_error(b->core));
+    if (fits) *fits = true;
     if (b->n_bh > 0) {
         int32_t h[TC_COUNT];
         rc = read_tree_counts(b, h);
         if (rc) return rc;
-        if (h[TC_OVERFLOW] != 0 || h[TC_HASHFAIL] != 0)
-            return bfail(b, NB_ENOMEM, "batched octree exceeded its capacity; commit again to resize");
+        if (!tree_counts_fit(b, h)) {
+            if (fits) *fits = false;
+            else return bfail(b, NB_ENOMEM, "the batched octree outgrew its arrays");
+        }
     }
     return NB_OK;
 }
@@ -386,6 +401,8 @@ int batch_launch_steps(nb_batch* b, float dt, int nsteps) {
         int rc = build_graph(b, dt);
         if (rc) return rc;
     }
+    NB_BCUDA(b, cudaMemsetAsync(b->held, 0, sizeof(int), b->core->stream));
+    b->pending_dt = dt;
     for (int k = 0; k < nsteps; ++k) {
         NB_BCUDA(b, cudaGraphLaunch(b->exec, b->core->stream));
         b->core->prof.launches += b->graph_kernels;
@@ -393,10 +410,24 @@ int batch_launch_steps(nb_batch* b, float dt, int nsteps) {
     return NB_OK;
 }
 
+// Steps held because the octree outgrew its arrays (positions evolved, or a
+// new state was written) are the last ones of the launch: the tree is sized
+// again from the current state and they run once more.
 int batch_wait(nb_batch* b) {
     if (!b) return NB_EINVAL;
     cudaSetDevice(b->core->dev);
-    return sync_check(b);
+    for (int attempt = 0;; ++attempt) {
+        int rc = nb_synchronize(b->core);
+        if (rc) return bfail(b, rc, nb_last_error(b->core));
+        int held = 0;
+        NB_BCUDA(b, cudaMemcpy(&held, b->held, sizeof(int), cudaMemcpyDeviceToHost));
+        if (held == 0) return sync_check(b);
+        if (attempt == 3) return bfail(b, NB_ENOMEM, "the batched octree kept outgrowing its arrays");
+        rc = size_tree(b);
+        if (rc) return rc;
+        rc = batch_launch_steps(b, b->pending_dt, held);
+        if (rc) return rc;
+    }
 }
 
 }  // namespace nb
@@ -423,7 +454,7 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
         b->bh_theta = bh_theta;
         b->far_eta = 0.025 / (bh_theta * bh_theta * bh_theta);
         b->core = core;
-        if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess) {
+        if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess || cudaMalloc(&b->held, sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
             nb_batch_destroy(b);
             return NB_ENOMEM;
@@ -443,7 +474,7 @@ int nb_batch_destroy(nb_batch* b) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
         void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
                         b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
-                        b->unit_comp, b->part, b->next_unit};
+                        b->unit_comp, b->part, b->next_unit, b->held};
         for (void* p : ptrs) cudaFree(p);
         if (b->core) nb_destroy(b->core);
         delete b;
@@ -648,8 +679,15 @@ int nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3) {
         cudaSetDevice(b->core->dev);
         int rc = enqueue_step(b, 0.f, false);
         if (rc) return rc;
-        rc = sync_check(b);
+        bool fits = true;
+        rc = sync_check(b, &fits);
         if (rc) return rc;
+        if (!fits) {   // the tree outgrew its arrays: size it from this state and evaluate again
+            rc = size_tree(b);
+            if (!rc) rc = enqueue_step(b, 0.f, false);
+            if (!rc) rc = sync_check(b);
+            if (rc) return rc;
+        }
         nb_sim* c = b->core;
         std::vector<float4> a(g->n), p(g->n);
         NB_BCUDA(b, cudaMemcpy(a.data(), c->acc + g->off, g->n * 16, cudaMemcpyDeviceToHost));
@@ -725,6 +763,10 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
         if (!b->committed) return bfail(b, NB_EBADSTATE, "nb_batch_commit first");
         if (trial_steps < 1) return bfail(b, NB_EINVAL, "trial_steps >= 1");
         cudaSetDevice(b->core->dev);
+        // the trials step from the current state: size the tree for it (a state
+        // written since the commit may need more nodes)
+        int rc = size_tree(b);
+        if (rc) return rc;
         nb_sim* c = b->core;
         const size_t bytes = c->n_pad * sizeof(float4);
         float4* save = nullptr;
@@ -757,7 +799,6 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
         };
         nb_tuning best = b->tune;
         float best_ms = INFINITY;
-        int rc = NB_OK;
         const int leafs[] = {8, 16, 32, 64};
         for (int ls : (b->n_bh > 0 ? std::vector<int>(leafs, leafs + 4) : std::vector<int>{best.leaf_size})) {
             nb_tuning t = best;

@@ -244,7 +244,7 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
     __stcg(&cell_walk[c], walk_record(F, count, int_first[k], BK_INTERNAL, nch, level));
 }
 
-__global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_dev,
+__global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ counters,
                                 const int32_t* __restrict__ int_parent, const int32_t* __restrict__ int_nint,
                                 int32_t* __restrict__ int_pending, const int32_t* __restrict__ int_cell,
                                 const int32_t* __restrict__ int_block, const uint32_t* __restrict__ int_mask,
@@ -255,7 +255,8 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_d
                                 const float4* __restrict__ cell_hi, int cell_cap, int nbodies,
                                 int* __restrict__ err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ni = min(*n_int_dev, int_cap);
+    if (!tree_fits(counters, int_cap, cell_cap)) return;   // held step: no moments
+    const int ni = min(counters[TC_NINT], int_cap);
     if (k >= ni || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {
         finish_moments(k, int_cell, int_block, int_mask, int_first, spos, cell_com, cell_q1, cell_q2, cell_count,
@@ -275,10 +276,11 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ n_int_d
 // galaxy's first sorted position.
 __global__ void k_batch_roots(const int32_t* __restrict__ slot_start, int nslot, const uint64_t* __restrict__ keys,
                               const int32_t* __restrict__ int_base, const int32_t* __restrict__ int_cell,
-                              const int32_t* __restrict__ n_int_dev, int int_cap, int32_t* __restrict__ root,
-                              int32_t* __restrict__ err) {
+                              const int32_t* __restrict__ counters, int int_cap, int cell_cap,
+                              int32_t* __restrict__ root, int32_t* __restrict__ err) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nslot) return;
+    if (!tree_fits(counters, int_cap, cell_cap)) return;   // held step: no walk
     const int s = slot_start[g];
     int prev = -1;
     if (s > 0) {
@@ -286,7 +288,7 @@ __global__ void k_batch_roots(const int32_t* __restrict__ slot_start, int nslot,
         prev = x == 0 ? kBatchDepth : (__clzll((long long)x) - (64 - 3 * kBatchDepth)) / 3;
     }
     const int k = int_base[s] + (kSlotLevels - (prev + 1));
-    if (prev + 1 > kSlotLevels || k < 0 || k >= min(*n_int_dev, int_cap)) {
+    if (prev + 1 > kSlotLevels || k < 0 || k >= min(counters[TC_NINT], int_cap)) {
         root[g] = -1;
         record_error(err, DEV_TREE_OVERFLOW);
         return;
@@ -327,12 +329,14 @@ __device__ __forceinline__ bool groupable(int level, int count) {
     return count <= kGroupMax && level >= kSlotLevels + kGroupMinDepth;
 }
 
-__global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ n_int_dev, const int32_t* __restrict__ int_cell,
+__global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ counters, const int32_t* __restrict__ int_cell,
                                const int4* __restrict__ cell_walk, const int32_t* __restrict__ sorder,
                                const int32_t* __restrict__ body_slot, int n_cells, int nbodies,
                                int4* __restrict__ groups, int cap, int* __restrict__ n_groups, int* __restrict__ err) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= min(*n_int_dev, int_cap)) return;
+    // a held step emits no groups, so the traversal after it has no work
+    if (!tree_fits(counters, int_cap, n_cells)) return;
+    if (k >= min(counters[TC_NINT], int_cap)) return;
     const int c = int_cell[k];
     if (c < 0 || c >= n_cells) {
         record_error(err, DEV_TREE_OVERFLOW);

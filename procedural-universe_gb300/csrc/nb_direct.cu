@@ -213,9 +213,14 @@ __global__ void k_direct_reduce_update(const float4* __restrict__ part, int spli
 __global__ void k_kick_drift(const float4* __restrict__ acc, int n, float4* __restrict__ pos,
                              float4* __restrict__ posc, float4* __restrict__ vel, float4* __restrict__ velc,
                              float dt, float inv_scale, int comp, nb_render_vertex* __restrict__ rv,
-                             const float4* __restrict__ rcol, float rscale) {
+                             const float4* __restrict__ rcol, float rscale, const int32_t* __restrict__ hold,
+                             int int_cap, int cell_cap, int* __restrict__ held) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (hold && !tree_fits(hold, int_cap, cell_cap)) {   // the step is held: the state stays as it was
+        if (i == 0) atomicAdd(held, 1);
+        return;
+    }
     const float4 a = acc[i];
     float4 v = vel[i], vc = velc[i], x = pos[i], xc = posc[i];
     if (comp) {
@@ -346,13 +351,14 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     return cudaGetLastError();
 }
 
-cudaError_t kick_drift(nb_sim* sim, float dt) {
+cudaError_t kick_drift(nb_sim* sim, float dt, const int32_t* hold, int int_cap, int cell_cap, int* held) {
     const int n = (int)sim->n;
     const bool comp = !(sim->prm.flags & NB_FLAG_NO_COMPENSATION);
     PhaseScope ps(sim, 7);
     k_kick_drift<<<(n + 255) / 256, 256, 0, sim->stream>>>(sim->acc, n, sim->pos, sim->posc, sim->vel, sim->velc,
                                                            dt, (float)(1.0 / sim->prm.pos_scale), comp ? 1 : 0,
-                                                           sim->render, sim->rcolour, sim->rscale);
+                                                           sim->render, sim->rcolour, sim->rscale, hold, int_cap,
+                                                           cell_cap, held);
     return cudaGetLastError();
 }
 

@@ -94,6 +94,17 @@ enum : int {
     TC_COUNT = 8
 };
 
+#ifdef __CUDACC__
+// Whether a tree built over fixed capacities (int_cap internal nodes,
+// cell_cap cells) without a host check of its counts fits them.  The counts
+// are final once the topology kernels have run.
+__device__ __forceinline__ bool tree_fits(const int32_t* counters, int int_cap, int cell_cap) {
+    const int ni = counters[TC_NINT];
+    return (counters[TC_OVERFLOW] | counters[TC_HASHFAIL]) == 0 && ni <= int_cap &&
+           ni + counters[TC_NLEAF] <= cell_cap;
+}
+#endif
+
 // Phases timed by the per-handle profiler (NB_PHASE_* in the public header).
 constexpr int kPhases = 10;
 
@@ -174,7 +185,10 @@ int direct_splits(const nb_sim* sim, const DirectTuning& t, size_t n_pad);
 size_t direct_part_entries(const nb_sim* sim, const DirectTuning& t, size_t n_pad);
 
 // Generic kick-drift of bodies from sim->acc (used after a Barnes-Hut force pass).
-cudaError_t kick_drift(nb_sim* sim, float dt);
+// hold (device tree counters, optional): a step whose tree does not fit
+// int_cap / cell_cap leaves the state unchanged and adds one to *held.
+cudaError_t kick_drift(nb_sim* sim, float dt, const int32_t* hold = nullptr, int int_cap = 0, int cell_cap = 0,
+                       int* held = nullptr);
 
 // ---- FP64 oracle and diagnostics (nb_fp64.cu) ----
 cudaError_t fp64_forces(nb_sim* sim, const int32_t* d_targets, size_t m, double* d_out3);

@@ -210,3 +210,33 @@ def test_full_size_config4_error_bounds():
                 assert O.rel_l2(b.forces(g), plain_direct_forces(pm, v)) < DIRECT_TOL, (g, n)
                 direct_checked += 1
         assert direct_checked >= 10
+
+
+def test_octree_outgrowing_its_arrays_is_resized_and_steps_rerun():
+    """The batched octree's arrays are sized at commit (twice the counts then).
+    A state written into the committed batch whose octree needs far more nodes
+    (every body with a partner 1e-4 away: long chains of internal nodes) makes
+    the steps on that tree hold -- state unchanged -- until the wait resizes
+    the tree and runs them again: the result equals a batch committed with
+    that state."""
+    gals = [galaxies()[k] for k in (4, 5, 0)]   # two Barnes-Hut members, one direct-sum member
+    pairs = []
+    for pm, v in gals:
+        n = len(pm)
+        q = pm.copy()
+        half = (n + 1) // 2
+        q[half:, :3] = pm[: n - half, :3] + np.float32(1e-4)
+        pairs.append((q, v.copy()))
+    with make_batch(gals) as a:
+        a.step(1e-3, 2)
+        before = a.tree_stats()["internal"]
+        a.write_state(np.concatenate([p for p, _ in pairs]), np.concatenate([w for _, w in pairs]))
+        a.step(1e-3, 3)
+        assert a.tree_stats()["internal"] > 2 * before
+        with make_batch(pairs) as b:
+            b.step(1e-3, 3)
+            for g in range(len(gals)):
+                pa, va = a.read(g)
+                pb, vb = b.read(g)
+                np.testing.assert_array_equal(pa, pb)
+                np.testing.assert_array_equal(va, vb)
