@@ -256,10 +256,10 @@ int ensure_state(nb_sim* s, size_t n) {
     return NB_OK;
 }
 
-int check_device_error(nb_sim* s) {
-    NB_CUDA(s, cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    NB_CUDA(s, cudaStreamSynchronize(s->stream));
-    const int code = *s->h_err;
+// The device error word as copied to h_err[0] by a copy queued before the
+// caller's last synchronisation of the stream.
+int decode_device_error(nb_sim* s) {
+    const int code = s->h_err[0];
     if (code == DEV_OK) return NB_OK;
     NB_CUDA(s, cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
     switch (code) {
@@ -269,6 +269,12 @@ int check_device_error(nb_sim* s) {
         case DEV_BAD_INPUT: return fail(s, NB_EINVAL, "non-finite value in the particle state");
         default: return fail(s, NB_ECUDA, "device error code " + std::to_string(code));
     }
+}
+
+int check_device_error(nb_sim* s) {
+    NB_CUDA(s, cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    NB_CUDA(s, cudaStreamSynchronize(s->stream));
+    return decode_device_error(s);
 }
 
 int force_pass(nb_sim* s, float dt, bool update) {
@@ -391,7 +397,7 @@ int nb_create(const nb_params* params, nb_sim** out) {
             if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return NB_ECUDA; }
             s->own_stream = true;
         }
-        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, sizeof(int)) != cudaSuccess ||
+        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 2 * sizeof(int)) != cudaSuccess ||
             cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess) {
             cudaGetLastError();
             nb_destroy(s);
@@ -399,7 +405,7 @@ int nb_create(const nb_params* params, nb_sim** out) {
         }
         cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
         cudaMemsetAsync(s->d_inter, 0, sizeof(unsigned long long), s->stream);
-        *s->h_err = 0;
+        s->h_err[0] = s->h_err[1] = 0;
         *out = s;
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed
@@ -482,13 +488,15 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
                                                                             d_any, s->d_err);
         e = cudaGetLastError();
     }
+    // the force flag and the error word come back with one synchronisation
     int any = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, d_any, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err + 1, d_any, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) any = *s->h_err;
+    if (e == cudaSuccess) any = s->h_err[1];
     if (e != cudaSuccess) return cuda_fail(s, e, host ? "nb_init_particles" : "nb_init_seeded");
     s->finit_pending = any != 0;
-    rc = check_device_error(s);
+    rc = decode_device_error(s);
     if (rc) { s->n = 0; return rc; }
     return NB_OK;
 }
@@ -612,9 +620,10 @@ int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
             k_writeback_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(
                 s->pos, s->vel, s->velc, s->acc, (int)n, zero, reinterpret_cast<uint32_t*>(particles));
             cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
             if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
-            return check_device_error(s);
+            return decode_device_error(s);
         }
         WbRecord* d_wb = static_cast<WbRecord*>(device_stage(s, n * sizeof(WbRecord)));
         WbRecord* h_wb = static_cast<WbRecord*>(host_stage(s, n * sizeof(WbRecord)));
@@ -623,9 +632,10 @@ int nb_write_back(nb_sim* s, nb_particle* particles, size_t n) {
                                                                             (int)n, zero, d_wb);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(h_wb, d_wb, n * sizeof(WbRecord), cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         if (e != cudaSuccess) return cuda_fail(s, e, "nb_write_back");
-        int rc = check_device_error(s);
+        int rc = decode_device_error(s);
         if (rc) return rc;
         auto scatter = [&](size_t b, size_t end) {
             for (size_t i = b; i < end; ++i) {

@@ -165,7 +165,7 @@ struct nb_sim {
     double* dscratch = nullptr;
     size_t dscratch_cap = 0;
     int* d_err = nullptr;     // device error word
-    int* h_err = nullptr;     // pinned mirror
+    int* h_err = nullptr;     // pinned: [0] mirror of d_err, [1] init's non-zero-force flag
     unsigned long long* d_inter = nullptr;
     uint64_t inter_last = 0;
     bool forces_fresh = false;  // acc holds the forces of the current positions
