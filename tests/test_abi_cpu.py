@@ -177,3 +177,21 @@ def test_server_release_of_rejected_and_unknown_jobs():
             s.release(queued)
         with pytest.raises(nb.NBodyError):
             s.release(12345)
+
+
+def test_server_retries_a_failed_batch_build():
+    """Host logic of the serving loop: when the batch cannot be built (here,
+    on a machine without a usable GPU, nb_batch_create fails) the admitted job
+    stays active with no steps done, and the next tick tries the build again
+    instead of stepping a batch that does not hold the job."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("the batch builds on a machine with a GPU")
+    import nbody_serve as ns
+    with ns.NBodyServer() as s:
+        j = s.submit(1, 1000, 10, 1e-3, 0)
+        for _ in range(2):
+            with pytest.raises(nb.NBodyError, match="nb_batch_create"):
+                s.tick()
+            st = s.status(j)
+            assert st["state"] == 1 and st["steps_done"] == 0
