@@ -22,14 +22,22 @@ Workloads (seeded synthetic galaxies; no dataset is involved):
               batching under a memory budget)
   bh1m_batched  the batched form (group traversal, quadrupoles) on the bh1m galaxy
 
-The default line (bh1m, one GPU) also carries "forms": the batched and the
-served form on their workloads, each against sequential plain-path launches
-at the plain path's own theta and at equal accuracy (force error <= 1e-3
-against the FP64 direct sum); --no-forms leaves them out.
+The default line (bh1m, one GPU) also carries
+  "direct": the two direct-sum configurations, direct262k (20 steps) and
+            direct4096 (100 steps), each with its own roofline against the
+            FP32 FMA peak, FP64 force error, drift, CPU baseline and e2e
+            (--no-direct leaves them out);
+  "forms":  the batched and the served form on their workloads, each against
+            sequential plain-path launches at the plain path's own theta and
+            at equal accuracy (force error <= 1e-3 against the FP64 direct
+            sum) (--no-forms leaves them out).
 
 --impl reference times the reference's CPU algorithm (the oracle's
 restatement of BruteForceCPU / BarnesHut on all host cores) on the same
-workload, a bounded sample per step.
+workload, a bounded sample per step.  That arm loads only the oracle's
+library: its initial states come from the oracle's copy of the workload
+generator (the same source as the product's nb_seed_*, byte-identical
+output), and it does not build or load the CUDA library.
 Multi-GPU: the step does not shard across GPUs; --gpus N runs N
 independent replicas (one galaxy per rank, different seeds) and reports the
 aggregate.
@@ -68,13 +76,28 @@ L2_FLUSH_BYTES = 512 << 20       # > 129 MB L2
 FLOP_PER_INTERACTION = 20
 
 
-def seed_workload(w, seed):
-    import nbody_gb300 as nb
+# the step count each configuration is specified with (its sub-line in the default run)
+CONFIG_STEPS = {"bh1m": 50, "direct262k": 20, "direct4096": 100}
+
+
+def seed_workload(w, seed, gen=None):
+    """Initial state (pos+mass, velocity) of workload w.  gen is the module
+    whose seeders are used: the product binding for the GPU arm, the oracle
+    for the CPU arm; both compile the same generator source."""
+    if gen is None:
+        import nbody_gb300 as gen
     if w["model"] == "disk":
-        return nb.seed_disk(seed, w["n"])
+        return gen.seed_disk(seed, w["n"])
     if w["model"] == "collision":
-        return nb.seed_collision(seed, w["n"])
-    return nb.seed_plummer(seed, w["n"])
+        return gen.seed_collision(seed, w["n"])
+    return gen.seed_plummer(seed, w["n"])
+
+
+def workload_config(name, w, world):
+    """The line's config object; identical for both arms of the same run."""
+    return {"workload": name, "desc": w["desc"], "n": w["n"],
+            "parallelism": "replicas" if world > 1 else "1 GPU",
+            "l2": "flushed (512 MB write) before every timed step"}
 
 
 def dist_env():
@@ -221,11 +244,15 @@ def cpu_baseline(w, pm, v, budget_s=12.0, F_gpu=None):
     return out
 
 
-def run_reference(args, w):
+def run_reference(args, name, w):
+    """The reference arm: the oracle's restatement of the reference's CPU
+    algorithm on all host cores, a bounded sample of the workload per step.
+    Loads only oracle/_build/libnb_oracle.so (no CUDA library)."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
-    pm, v = seed_workload(w, 1234)
+    from oracle import oracle as O
+    pm, v = seed_workload(w, replica_seed(0), gen=O)
     vals = []
     base = None
     for i in range(args.warmup + args.steps):
@@ -237,7 +264,7 @@ def run_reference(args, w):
     out = {"metric": METRIC, "value": val, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * w["n"] / val if val else None,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-           "data": "synthetic (seeded)", "config": {"workload": args.workload, "desc": w["desc"], "n": w["n"]},
+           "data": "synthetic (seeded galaxies)", "config": workload_config(name, w, args.gpus),
            "cpu_baseline": {"value": val, "unit": METRIC, "cores": base["cores"] if base else None,
                             "kind": "port", "sample": base["sample"] if base else ""},
            "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -245,17 +272,24 @@ def run_reference(args, w):
     return 0
 
 
-# --------------------------------------------------------------------------
-def run_ours(args, w):
+# DRAM bytes per launch of the dominant kernels, from one ncu capture each
+# (dram__bytes_read.sum + dram__bytes_write.sum); the summaries under
+# profiles/ give the command and the figures.
+NCU_TRAFFIC = {
+    ("bh1m", "k_traverse"): (86.4e6, "profiles/k_traverse_bh1m.md"),
+    ("direct262k", "k_direct_force"): (267.1e6, "profiles/k_direct_force_direct262k.md"),
+}
+
+
+def measure(args, name, w, steps, warmup, world, rank, dev, with_cpu=True, with_e2e=True):
+    """One workload on the plain path: K timed steps with the state resident
+    (CUDA events on the simulator's stream, L2 flushed before each step), the
+    dominant kernel's roofline, FP64 force error and drift, e2e through the
+    C-ABI with pinned host records, and the CPU baseline (rank 0).  Returns
+    the line's fields."""
     import torch
     import nbody_gb300 as nb
 
-    world, rank, local = dist_env()
-    dev = local if world > 1 else 0
-    torch.cuda.set_device(dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     n = w["n"]
     pm, v = seed_workload(w, replica_seed(rank))
     stream = torch.cuda.Stream(device=dev)
@@ -270,7 +304,7 @@ def run_ours(args, w):
     diag0 = sim.diagnostics(0.0)       # FP64 energy and angular momentum of the initial state
 
     # warm-up (untimed)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         sim.step(dt, 1)
     sim.synchronize()
 
@@ -279,16 +313,15 @@ def run_ours(args, w):
     launches0 = ctypes.c_uint64(0)
     lib.nb_launch_count(sim.handle, ctypes.byref(launches0))
     lib.nb_profile_enable(sim.handle, 1)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     clocks = ClockSampler(dev)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
     t_wall0 = time.perf_counter()
-    inter_total = 0
     with torch.cuda.stream(stream):
-        for k in range(args.steps):
+        for k in range(steps):
             flush.zero_()                       # L2 flush between timed steps (untimed)
             evs[k][0].record(stream)
             sim.step(dt, 1)
@@ -311,13 +344,13 @@ def run_ours(args, w):
             phases[nm] = {"ms_total": ms.value, "launches": int(cnt.value), "ms_avg": ms.value / cnt.value}
     lib.nb_profile_enable(sim.handle, 0)
     total_ms = max_over_ranks(total_ms, device="cuda")
-    value = replicas_value(world, n, args.steps, total_ms)
+    value = replicas_value(world, n, steps, total_ms)
     # drift over the warm-up and timed steps (kick-drift velocities synchronised by half a kick)
     diag1 = sim.diagnostics(0.5 * dt)
     L0, L1 = diag0["angular_momentum"], diag1["angular_momentum"]
     drift = {"energy_rel": (diag1["total"] - diag0["total"]) / abs(diag0["total"]),
              "angular_momentum_rel": float(np.linalg.norm(L1 - L0) / max(np.linalg.norm(L0), 1e-300)),
-             "energy_initial": diag0["total"], "steps": args.warmup + args.steps, "dt": dt,
+             "energy_initial": diag0["total"], "steps": warmup + steps, "dt": dt,
              "how": "FP64 reductions on the GPU (kinetic + pairwise potential, L = sum m x × v)"}
 
     # ---- roofline of the dominant kernel ----
@@ -333,12 +366,17 @@ def run_ours(args, w):
     lib.nb_probe_fp32_peak(dev, ctypes.byref(fp32))
     flops = FLOP_PER_INTERACTION * float(inter_last)
     dom = "traverse" if w["kind"] == 2 else "direct_force"
+    kname = "k_traverse" if w["kind"] == 2 else "k_direct_force"
     ph = phases.get(dom, {})
     t_launch = ph.get("ms_avg", float("nan")) * 1e-3
     achieved = flops / t_launch / 1e12
-    roof = {"kernel": "k_traverse" if w["kind"] == 2 else "k_direct_force", "bound": "fp32", "achieved": achieved,
+    traffic = NCU_TRAFFIC.get((name, kname))
+    roof = {"kernel": kname, "bound": "fp32", "achieved": achieved,
             "peak": fp32.value, "unit": "TFLOP/s", "frac": achieved / fp32.value if fp32.value else None,
-            "traffic": None, "peak_source": "measured on this GPU by an FMA-chain probe (nb_probe_fp32_peak)",
+            "traffic": traffic[0] if traffic else None,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, " + traffic[1])
+            if traffic else None,
+            "peak_source": "measured on this GPU by an FMA-chain probe (nb_probe_fp32_peak)",
             "flops_per_launch": flops, "interactions_per_launch": float(inter_last),
             "launch_ms": t_launch * 1e3}
     if w["kind"] == 2:
@@ -352,13 +390,13 @@ def run_ours(args, w):
 
     # ---- end-to-end through the C-ABI with pinned host records ----
     e2e = None
-    if not args.no_e2e:
+    if with_e2e:
         nbytes = n * nb.PARTICLE_DTYPE.itemsize
         pinned = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
         buf = (ctypes.c_char * nbytes).from_address(pinned.data_ptr())
         host = np.frombuffer(buf, dtype=nb.PARTICLE_DTYPE, count=n)
         host[:] = rec_host
-        e2e_steps = max(1, min(args.steps, 5))
+        e2e_steps = max(1, min(steps, 5))
         sim.init(host)
         sim.step(dt, 1)
         sim.write_back(host)
@@ -380,34 +418,70 @@ def run_ours(args, w):
     F = sim.compute_forces()
     F64 = sim.fp64_forces(targets)
     ferr = float(np.linalg.norm(F[targets] - F64) / np.linalg.norm(F64))
+    sim.close()
 
-    if rank != 0:
-        return 0
     cpu = None
-    if not args.no_cpu_baseline:
+    if with_cpu and rank == 0:
         cpu = cpu_baseline(w, pm, v, F_gpu=F_init)
         cpu.pop("step_s", None)
-    forms = None
-    if world == 1 and not args.no_forms:
-        forms = run_forms(args)
     out = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": total_ms / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (Kahan-compensated) + f64 diagnostics",
         "data": "synthetic (seeded galaxies)",
-        "config": {"workload": args.workload, "desc": w["desc"], "n": n, "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "l2": "flushed (512 MB write) before every timed step"},
+        "config": workload_config(name, w, world),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches1.value - launches0.value),
         "clocks": clk,
         "interactions_per_step": inter_last,
-        "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)), "drift": drift,
-        "phases_ms_avg": {k: v_["ms_avg"] for k, v_ in phases.items()},
-        "wall_s_timed_region": t_wall,
-        "forms": forms,
+        "force_rel_l2_vs_fp64": ferr, "force_err_sample": int(len(targets)),
     }
-    print(json.dumps(out))
-    sim.close()
+    # The contract's tolerance: direct sum within 1e-5 of the FP64 direct sum;
+    # Barnes-Hut within 1e-3 of the reference's own CPU algorithm at the same
+    # theta and softening (its monopole, per-body rule errs by a few 1e-3
+    # against FP64 at theta = 0.5, which force_rel_l2_vs_fp64 shows).
+    if w["kind"] == 2:
+        vs_port = cpu.get("force_rel_l2_gpu_vs_port") if cpu else None
+        out["force_rel_l2_vs_reference_port"] = vs_port
+        out["force_tolerance"] = {
+            "against": "the reference's CPU Barnes-Hut (oracle restatement), same theta and softening, "
+                       "initial state, sampled bodies", "limit": 1e-3, "value": vs_port,
+            "met": (vs_port is not None and vs_port <= 1e-3),
+            "fp64_error_of_the_reference_algorithm": ferr}
+    else:
+        out["force_tolerance"] = {"against": "FP64 direct sum on the GPU, sampled bodies", "limit": 1e-5,
+                                  "value": ferr, "met": ferr <= 1e-5}
+    out["drift"] = drift
+    out["phases_ms_avg"] = {k: v_["ms_avg"] for k, v_ in phases.items()}
+    out["wall_s_timed_region"] = t_wall
+    return out
+
+
+def run_ours(args, name, w):
+    import torch
+
+    world, rank, local = dist_env()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    out = measure(args, name, w, args.steps, args.warmup, world, rank, dev,
+                  with_cpu=not args.no_cpu_baseline, with_e2e=not args.no_e2e)
+    if rank == 0:
+        if world == 1 and not args.no_direct and name == "bh1m":
+            # the direct-sum configurations, each over its configured step count
+            out["direct"] = {}
+            for sub in ("direct262k", "direct4096"):
+                d = measure(args, sub, WORKLOADS[sub], CONFIG_STEPS[sub], args.warmup, 1, 0, dev,
+                            with_cpu=not args.no_cpu_baseline, with_e2e=not args.no_e2e)
+                for k in ("metric", "unit", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data"):
+                    d.pop(k, None)
+                out["direct"][sub] = d
+        out["forms"] = None
+        if world == 1 and not args.no_forms:
+            out["forms"] = run_forms(args)
+        print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -421,13 +495,15 @@ def run_forms(args):
     import nbody_gb300 as nb
     import bench_forms
 
-    fargs = argparse.Namespace(steps=10, warmup=3, no_cpu_baseline=True)
+    # each form over its configured step count: 100 steps of the 512-galaxy
+    # batch, 200 steps per served job
+    fargs = argparse.Namespace(steps=bench_forms.BATCH_STEPS, warmup=3, no_cpu_baseline=True)
     out = {}
     b = bench_forms.run_batch(fargs, nb, torch)
     s = bench_forms.run_served(fargs, nb, torch)
     for name, r in (("batch512", b), ("served", s)):
         out[name] = {
-            "value": r["value"], "unit": r["unit"], "config": r["config"],
+            "value": r["value"], "unit": r["unit"], "steps": r["steps"], "config": r["config"],
             "force_rel_l2_vs_fp64": r.get("force_rel_l2_vs_fp64_max", r.get("force_rel_l2_vs_fp64_largest")),
             "sequential_plain": {k: r["sequential_plain"][k] for k in
                                  ("value", "theta", "force_rel_l2_vs_fp64_largest")},
@@ -457,8 +533,21 @@ def main():
                     help="jobs in the served workload's Poisson stream (--workload served)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched and served forms reported beside the plain-path line")
+    ap.add_argument("--no-direct", action="store_true",
+                    help="skip the direct-sum configurations reported beside the plain-path line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        # the CPU arm: the oracle only, neither built nor loaded CUDA library
+        if dist_env()[1] != 0:
+            return 0
+        if args.workload in ("batch512", "served"):
+            import bench_forms
+            from oracle import oracle as O
+            print(json.dumps(bench_forms.reference_line(args, O, args.workload)))
+            return 0
+        name = "bh1m" if args.workload == "bh1m_batched" else args.workload
+        return run_reference(args, name, WORKLOADS[name])
     import nb_build
     nb_build.build()
     if args.workload in ("batch512", "served", "bh1m_batched"):
@@ -467,19 +556,11 @@ def main():
         import bench_forms
         if dist_env()[1] != 0:
             return 0
-        if args.impl == "reference":
-            if args.workload == "bh1m_batched":
-                return run_reference(args, WORKLOADS["bh1m"])
-            print(json.dumps(bench_forms.reference_line(args, nb, args.workload)))
-            return 0
         fn = {"batch512": bench_forms.run_batch, "served": bench_forms.run_served,
               "bh1m_batched": bench_forms.run_batch_single}[args.workload]
         print(json.dumps(fn(args, nb, torch)))
         return 0
-    w = WORKLOADS[args.workload]
-    if args.impl == "reference":
-        return run_reference(args, w)
-    return run_ours(args, w)
+    return run_ours(args, args.workload, WORKLOADS[args.workload])
 
 
 if __name__ == "__main__":

@@ -24,6 +24,29 @@ import numpy as np
 
 METRIC = "body-steps/s"
 SERVED_REQUESTS = 200   # jobs in the served stream (mean n about 154,000, arrivals over about 1 s)
+BATCH_STEPS = 100       # steps of the 512-galaxy batch, as the workload specifies
+BATCH = dict(eps2=1e-4, dt=1e-3, theta=0.6, threshold=8192)
+SERVED = dict(rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005, max_active=64, steps_per_round=25,
+              round_seconds=0.1)
+
+
+def batch_config(gals):
+    """config object of the batch512 lines (both arms)."""
+    n_real = sum(pm.shape[0] for pm, _ in gals)
+    bh = sum(1 for pm, _ in gals if pm.shape[0] >= BATCH["threshold"])
+    return {"workload": "batch512", "galaxies": len(gals), "bodies": n_real,
+            "barnes_hut_members": bh, "theta": BATCH["theta"], "eps": 0.01, "dt": BATCH["dt"],
+            "l2": "inputs (%.0f MB of state) larger than L2" % (n_real * 64 / 1e6)}
+
+
+def served_config(requests, sizes, round_seconds):
+    """config object of the served lines (both arms)."""
+    c = SERVED
+    return {"workload": "served", "requests": requests, "rate_per_s": c["rate"], "n_range": [1024, 1 << 20],
+            "mean_n": float(sizes.mean()), "steps_per_job": c["steps"], "theta": c["theta"], "eps": c["eps"],
+            "dt": c["dt"], "memory_budget_gb": 120, "max_active": c["max_active"],
+            "steps_per_round": c["steps_per_round"], "round_seconds": round_seconds,
+            "warmup": "one server run of two small jobs (4,096 and 512 bodies, 3 steps) before the stream"}
 
 
 def batch_galaxies(nb, seed=2024, count=512, lo=256, hi=65536):
@@ -163,18 +186,21 @@ def served_stream(requests=SERVED_REQUESTS, rate=200.0):
     return arrivals, sizes
 
 
-def reference_line(args, nb, workload):
+def reference_line(args, gen, workload):
     """The reference's CPU algorithms (oracle restatement) on a bounded sample
-    of the batched or served workload, as the reference arm's JSON line."""
+    of the batched or served workload, as the reference arm's JSON line.  gen
+    is the oracle module: its copy of the workload generator gives the same
+    galaxies as the GPU arm's."""
     if workload == "batch512":
-        gals = batch_galaxies(nb)
-        cpu = cpu_sample(gals, 1e-4, 0.6, 8192)
-        cfg = {"workload": "batch512", "galaxies": len(gals)}
+        gals = batch_galaxies(gen)
+        cpu = cpu_sample(gals, BATCH["eps2"], BATCH["theta"], BATCH["threshold"])
+        cfg = batch_config(gals)
     else:
-        _, sizes = served_stream(getattr(args, "requests", SERVED_REQUESTS))
-        gals = [nb.seed_disk(10_000 + k, int(n)) for k, n in enumerate(sizes)]
-        cpu = cpu_sample(gals, 0.005 ** 2, 0.5, 1024, count=len(gals))
-        cfg = {"workload": "served", "requests": len(sizes)}
+        requests = getattr(args, "requests", SERVED_REQUESTS)
+        _, sizes = served_stream(requests, SERVED["rate"])
+        gals = [gen.seed_disk(10_000 + k, int(n)) for k, n in enumerate(sizes)]
+        cpu = cpu_sample(gals, SERVED["eps"] ** 2, SERVED["theta"], 1024, count=len(gals))
+        cfg = served_config(requests, sizes, SERVED["round_seconds"])
     return {"metric": METRIC, "value": cpu["value"], "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)", "config": cfg,
@@ -182,7 +208,8 @@ def reference_line(args, nb, workload):
             "e2e": {"value": cpu["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, theta=0.5, eps=0.005):
+def run_served(args, nb, torch, requests=None, rate=SERVED["rate"], steps=SERVED["steps"], dt=SERVED["dt"],
+               theta=SERVED["theta"], eps=SERVED["eps"]):
     import nbody_serve as ns
     if requests is None:
         requests = getattr(args, "requests", SERVED_REQUESTS)
@@ -274,11 +301,7 @@ def run_served(args, nb, torch, requests=None, rate=200.0, steps=200, dt=5e-4, t
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": steps,
         "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies, Poisson arrivals)",
-        "config": {"workload": "served", "requests": requests, "rate_per_s": rate, "n_range": [1024, 1 << 20],
-                   "mean_n": float(sizes.mean()), "steps_per_job": steps, "theta": theta, "eps": eps, "dt": dt,
-                   "memory_budget_gb": 120, "max_active": 64, "steps_per_round": 25,
-                   "round_seconds": server_round_s,
-                   "warmup": "one server run of two small jobs (4,096 and 512 bodies, 3 steps) before the stream"},
+        "config": served_config(requests, sizes, server_round_s),
         "offered": {"value": rate * float(sizes.mean()) * steps, "unit": METRIC},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
@@ -369,7 +392,7 @@ def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
 
 
 def run_batch(args, nb, torch):
-    eps2, dt, theta, threshold = 1e-4, 1e-3, 0.6, 8192
+    eps2, dt, theta, threshold = BATCH["eps2"], BATCH["dt"], BATCH["theta"], BATCH["threshold"]
     gals = batch_galaxies(nb)
     n_real = sum(pm.shape[0] for pm, _ in gals)
     stream = torch.cuda.Stream()
@@ -436,9 +459,7 @@ def run_batch(args, nb, torch):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (Kahan-compensated)", "data": "synthetic (seeded galaxies)", "gpu_launches": gpu_launches,
-        "config": {"workload": "batch512", "galaxies": len(gals), "bodies": n_real,
-                   "barnes_hut_members": len(bh_ids), "theta": theta, "eps": 0.01, "dt": dt,
-                   "l2": "inputs (%.0f MB of state) larger than L2" % (n_real * 64 / 1e6)},
+        "config": batch_config(gals),
         "sequential_plain": {"value": seq, "unit": METRIC, "theta": theta,
                              "force_rel_l2_vs_fp64_largest": plain_err,
                              "how": "one plain handle per galaxy, stepped one galaxy after another (2 steps each)"},

@@ -20,6 +20,13 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "nb_oracle.cpp")
+# The synthetic workload generator (seeded Plummer spheres, disk + bulge
+# galaxies, colliding spheres) is compiled into the oracle from the same
+# source file as the product's nb_seed_* so that the CPU arm of the bench
+# gets byte-identical initial states without loading the product library.
+# Its entry points are renamed orc_seed_* here.
+SEED_SRC = os.path.join(os.path.dirname(HERE), "procedural-universe_gb300", "csrc", "nb_seed.cpp")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libnb_oracle.so")
 
@@ -44,11 +51,14 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (-ffp-contract=off: float math as written)."""
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    deps = [SRC, SEED_SRC, os.path.join(os.path.dirname(SEED_SRC), "nb_rng.hpp")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     tmp = LIB + ".tmp.%d" % os.getpid()
+    rename = ["-Dnb_seed_plummer=orc_seed_plummer", "-Dnb_seed_disk=orc_seed_disk",
+              "-Dnb_seed_collision=orc_seed_collision"]
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-pthread", SRC, "-o", tmp]
+           "-pthread", *rename, "-I", INCLUDE, SRC, SEED_SRC, "-o", tmp]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -81,6 +91,10 @@ def lib():
             L.orc_fp64_forces.argtypes = [vp, vp, sz, vp, sz, dbl, dbl, i32, i32, vp]
             L.orc_fp64_diagnostics.argtypes = [vp, vp, vp, sz, dbl, dbl, i32, i32, vp]
             L.orc_threads_default.restype = i32
+            f64 = ctypes.c_double
+            L.orc_seed_plummer.argtypes = [ctypes.c_uint64, sz, f64, f64, vp, vp]
+            L.orc_seed_disk.argtypes = [ctypes.c_uint64, sz, f64, f64, f64, f64, f64, f64, vp, vp]
+            L.orc_seed_collision.argtypes = [ctypes.c_uint64, sz, f64, f64, f64, vp, vp]
             _lib = L
         return _lib
 
@@ -100,6 +114,29 @@ def particles_from_soa(pos_mass: np.ndarray, vel: np.ndarray | None = None) -> n
     p["colour"] = 1.0
     p["original_colour"] = 1.0
     return p
+
+
+# ---- workload generator (the same source as the product's nb_seed_*) -------
+
+def _seeded(fn, seed, n, *args):
+    pm = np.zeros((n, 4), np.float32)
+    v = np.zeros((n, 4), np.float32)
+    rc = fn(seed, n, *args, _ptr(pm), _ptr(v))
+    if rc:
+        raise RuntimeError("workload generator failed (%d)" % rc)
+    return pm, v
+
+
+def seed_plummer(seed: int, n: int, total_mass=1.0, a=1.0):
+    return _seeded(lib().orc_seed_plummer, seed, n, total_mass, a)
+
+
+def seed_disk(seed: int, n: int, total_mass=1.0, rd=1.0, z0=0.1, bulge_frac=0.1, ab=0.2, dispersion=0.05):
+    return _seeded(lib().orc_seed_disk, seed, n, total_mass, rd, z0, bulge_frac, ab, dispersion)
+
+
+def seed_collision(seed: int, n: int, a=1.0, separation=10.0, pericentre=1.0):
+    return _seeded(lib().orc_seed_collision, seed, n, a, separation, pericentre)
 
 
 def default_threads() -> int:
