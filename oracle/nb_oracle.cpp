@@ -6,12 +6,14 @@
  * baseline leg of bench.py).  Nothing in the product library links or calls
  * this file.
  *
- * PARITY UNPINNED: the reference (Procedural-Universe) holds no tests,
- * golden vectors or fixtures for this path (its test/ covers only logging
- * and Maths::ClosestParticle), and it cannot be compiled here (Windows/MSVC,
- * D3D11 and the un-vendored DirectXTK library).  This restatement follows
- * the cited reference lines; it is pinned by analytic known-answer tests
- * (tests/test_oracle_cpu.py) only.
+ * Pinned to the reference's own code: the reference (Procedural-Universe)
+ * holds no tests or golden vectors for this path, but its CPU simulator
+ * sources compile unmodified against type-only stand-ins for the DirectXTK
+ * and Direct3D headers (oracle/ref/Makefile), and this restatement is
+ * bit-identical to that build on every octree node, force and updated
+ * record (tests/test_reference_pin_cpu.py), apart from the two deviations
+ * below that change results (1 and 2).  The SimpleMath arithmetic stays
+ * unpinned: both sides compute it as the plain float operations below.
  *
  * Restated reference code:
  *   Phys::Gravity          src/Sim/Physics.hpp:25-47

@@ -5,9 +5,15 @@ N-body step (BruteForceCPU, BarnesHut/Octree, Phys::Gravity).  Only the tests,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import
 this module; the product library never does.
 
-PARITY UNPINNED: the reference has no golden vectors or tests for this path
-and cannot be compiled here (Windows/MSVC, D3D11, un-vendored DirectXTK); the
-restatement is pinned by analytic known-answer tests only.
+Pinned to the reference's own code: oracle/ref/Makefile compiles the
+reference's src/Sim/Octree.cpp, BarnesHut.cpp and BruteForceCPU.cpp
+unmodified against type-only stand-ins for the DirectXTK / Direct3D headers,
+and tests/test_reference_pin_cpu.py finds this restatement bit-identical to
+it (every octree node, every force, every updated record) wherever the
+depth cap and the remainder-slice fix do not apply; the committed vectors
+tests/golden/reference_small.npz come from that build.  Still unpinned: the
+DirectXTK SimpleMath arithmetic itself (the stand-in computes each vector
+operation in plain float in the documented order).
 """
 from __future__ import annotations
 
