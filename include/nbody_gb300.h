@@ -236,8 +236,12 @@ int  nb_profile_read(nb_sim* sim, int phase, double* total_ms, uint64_t* launche
 /* Launch tuning of a handle's kernels (results are unchanged up to FP32
  * summation order).  Keys: "direct_block" (64, 128, 256 threads),
  * "direct_ipt" (1, 2, 4, 8 target bodies per thread), "direct_splits"
- * (source ranges per target block, 0 = automatic).  Returns NB_EINVAL for
- * an unknown key or value. */
+ * (source ranges per target block, 0 = automatic), "wait_polls" (polls of
+ * each source-tile wait of the direct-sum force kernel before the step is
+ * abandoned, 0..4194304, default 4194304; lower values exist only to test the
+ * timeout path: the step then leaves the state unchanged and the next
+ * nb_synchronize returns NB_ETIMEOUT).  Returns NB_EINVAL for an unknown key
+ * or value. */
 int  nb_tune(nb_sim* sim, const char* key, int value);
 int  nb_get_tune(nb_sim* sim, const char* key, int* value);
 /* Kernel launches issued by this handle since creation. */
@@ -270,7 +274,19 @@ const char* nb_batch_last_error(const nb_batch* b);
 /* Adds one galaxy (host buffers n x float4 each, 1 <= n <= 16 Mi = 16,777,216);
  * galaxy receives its index. */
 int  nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t n, int32_t* galaxy);
-/* Uploads every galaxy, lays out the tables and sizes the tree buffers. */
+/* Adds one galaxy that nb_batch_commit generates on the device, straight into
+ * the batch's arrays (no host buffers): model 0 exponential disk + 10%
+ * Hernquist bulge (nb_seed_disk's defaults), 1 Plummer sphere
+ * (nb_seed_plummer's defaults), 2 two Plummer spheres on a parabolic orbit
+ * (nb_seed_collision's defaults); 2 <= n <= 16 Mi.  The bodies are those of
+ * the host generator of the same (model, seed, n) up to the rounding of the
+ * device math functions and of the centre-of-mass sum; a galaxy is the same
+ * in every batch and on every run.  The step before the path in the
+ * reference: its seeders fill the particle vector on the host
+ * (src/Sim/GalaxySeeder.cpp:43-144). */
+int  nb_batch_add_generated(nb_batch* b, int model, uint64_t seed, size_t n, int32_t* galaxy);
+/* Uploads (or generates) every galaxy, lays out the tables and sizes the tree
+ * buffers. */
 int  nb_batch_commit(nb_batch* b);
 int  nb_batch_set_tuning(nb_batch* b, const nb_tuning* t);
 /* Far field of the group traversal: an accepted cell farther from a group's
@@ -288,6 +304,11 @@ int  nb_batch_autotune(nb_batch* b, float dt, int trial_steps);
  * tree outgrows them leave the state unchanged on the device, and the call sizes
  * the tree from the current state and runs those steps again before it returns. */
 int  nb_batch_step(nb_batch* b, float dt, int nsteps);
+/* After nb_batch_step returned NB_ENOMEM because the octree kept outgrowing
+ * its arrays: how many of the nsteps requested were not run (they are the
+ * last ones; the state is nsteps - *steps steps ahead of where the call found
+ * it).  0 after a call that succeeded. */
+int  nb_batch_steps_not_run(nb_batch* b, int* steps);
 int  nb_batch_read(nb_batch* b, int32_t galaxy, float* pos_mass4, float* vel4);
 /* Forces (n x 3 doubles) of one galaxy at the current state. */
 int  nb_batch_forces(nb_batch* b, int32_t galaxy, double* force3);
@@ -346,7 +367,8 @@ int  nb_server_default_params(nb_server_params* p);
 int  nb_server_create(const nb_server_params* p, nb_server** out);
 int  nb_server_destroy(nb_server* s);
 const char* nb_server_last_error(const nb_server* s);
-/* Queues a job; its initial conditions are generated when it is admitted.  A job
+/* Queues a job; its initial conditions are generated on the device, straight
+ * into the batch's arrays, when it is admitted (nb_batch_add_generated).  A job
  * of more than 16 Mi bodies (the batched form's galaxy limit) or of more
  * estimated bytes than memory_budget can never run: it is recorded with
  * state -1 (rejected) and the call returns NB_OK. */
@@ -368,7 +390,10 @@ int  nb_server_stats(nb_server* s, uint64_t* body_steps, uint64_t* rounds);
 /* Where the server's time went: batch rebuilds (count, seconds: new batch,
  * hand-over, upload, tree sizing), stepping (seconds, steps of the batch, kernel
  * launches of those steps), and host generation of initial conditions
- * (seconds). Any pointer may be NULL. */
+ * (seconds; always 0: jobs are generated on the device, inside the
+ * rebuilds). Any pointer may be NULL.  A round that returned NB_ENOMEM
+ * because the octree kept outgrowing its arrays counts only the steps it
+ * ran, in the jobs' steps_done as here. */
 int  nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64_t* batch_steps, double* step_s,
                       double* generate_s, uint64_t* step_launches);
 

@@ -55,11 +55,15 @@ int cuda_fail(nb_sim* s, cudaError_t e, const char* where) {
 // Unpacks reference records into the SoA state; flags non-finite input.
 __global__ void k_unpack_records(const nb_particle* __restrict__ in, int n, int kind, float4* __restrict__ pos,
                                  float4* __restrict__ posc, float4* __restrict__ vel, float4* __restrict__ velc,
-                                 float4* __restrict__ finit, int* __restrict__ any_force, int* __restrict__ err) {
+                                 float4* __restrict__ finit, int* __restrict__ any_force, int* __restrict__ err,
+                                 unsigned* __restrict__ mmax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const nb_particle& p = in[i];
     const float m = (float)p.mass;
+    if (isfinite(m)) atomicMax(mmax, __float_as_uint(fabsf(m)));
+    const float ext = fmaxf(fmaxf(fabsf(p.position[0]), fabsf(p.position[1])), fabsf(p.position[2]));
+    if (isfinite(ext)) atomicMax(mmax + 1, __float_as_uint(ext));
     pos[i] = make_float4(p.position[0], p.position[1], p.position[2], m);
     posc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     vel[i] = make_float4((float)p.velocity[0], (float)p.velocity[1], (float)p.velocity[2], 0.f);
@@ -82,14 +86,22 @@ __global__ void k_unpack_records(const nb_particle* __restrict__ in, int n, int 
     }
 }
 
+// Validates a state written by a copy (finite values), clears its
+// compensation and records its largest |mass| in mmax[0] and its largest
+// |coordinate| in mmax[1] (the caller cleared both).
 __global__ void k_check_soa(const float4* __restrict__ pos, const float4* __restrict__ vel, int n,
-                            float4* __restrict__ posc, float4* __restrict__ velc, int* __restrict__ err) {
+                            float4* __restrict__ posc, float4* __restrict__ velc, int* __restrict__ err,
+                            unsigned* __restrict__ mmax) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = pos[i], v = vel[i];
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(p.w) && isfinite(v.x) && isfinite(v.y) &&
           isfinite(v.z)))
         record_error(err, DEV_BAD_INPUT);
+    else {
+        atomicMax(mmax, __float_as_uint(fabsf(p.w)));
+        atomicMax(mmax + 1, __float_as_uint(fmaxf(fmaxf(fabsf(p.x), fabsf(p.y)), fabsf(p.z))));
+    }
     posc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     velc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
@@ -319,11 +331,22 @@ int sim_reserve_zeroed(nb_sim* s, size_t n) {
     return ensure_state(s, n);
 }
 
+int sim_rescan_state(nb_sim* s) {
+    cudaSetDevice(s->dev);
+    if (s->n == 0) return NB_OK;
+    NB_CUDA(s, cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream));
+    k_check_soa<<<(unsigned)((s->n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)s->n, s->posc, s->velc,
+                                                                      s->d_err, s->d_mmax);
+    NB_CUDA(s, cudaGetLastError());
+    return NB_OK;
+}
+
 int sim_check_state(nb_sim* s) {
     cudaSetDevice(s->dev);
     if (s->n == 0) return NB_OK;
+    NB_CUDA(s, cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream));
     k_check_soa<<<(unsigned)((s->n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)s->n, s->posc, s->velc,
-                                                                      s->d_err);
+                                                                      s->d_err, s->d_mmax);
     NB_CUDA(s, cudaGetLastError());
     const int rc = check_device_error(s);
     if (rc) s->n = 0;
@@ -398,13 +421,15 @@ int nb_create(const nb_params* params, nb_sim** out) {
             s->own_stream = true;
         }
         if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 2 * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess) {
+            cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMalloc(&s->d_mmax, 2 * sizeof(unsigned)) != cudaSuccess) {
             cudaGetLastError();
             nb_destroy(s);
             return NB_ENOMEM;
         }
         cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
         cudaMemsetAsync(s->d_inter, 0, sizeof(unsigned long long), s->stream);
+        cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream);
         s->h_err[0] = s->h_err[1] = 0;
         *out = s;
         return NB_OK;
@@ -426,6 +451,7 @@ int nb_destroy(nb_sim* s) {
         cudaFree(s->dscratch);
         cudaFree(s->d_err);
         cudaFree(s->d_inter);
+        cudaFree(s->d_mmax);
         if (s->h_err) cudaFreeHost(s->h_err);
         if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
         delete s;
@@ -482,10 +508,11 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
             e = cudaMemcpyAsync(records_out, d_rec, n * sizeof(nb_particle), cudaMemcpyDeviceToHost, s->stream);
     }
     if (e == cudaSuccess) e = cudaMemsetAsync(d_any, 0, sizeof(int), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream);
     if (e == cudaSuccess) {
         k_unpack_records<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(src, (int)n, s->prm.kind, s->pos,
                                                                             s->posc, s->vel, s->velc, s->finit,
-                                                                            d_any, s->d_err);
+                                                                            d_any, s->d_err, s->d_mmax);
         e = cudaGetLastError();
     }
     // the force flag and the error word come back with one synchronisation
@@ -536,7 +563,9 @@ int nb_init_soa(nb_sim* s, const float* pos_mass4, const float* vel4, size_t n) 
         if (n == 0) return NB_OK;
         NB_CUDA(s, cudaMemcpyAsync(s->pos, pos_mass4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
         NB_CUDA(s, cudaMemcpyAsync(s->vel, vel4, n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
-        k_check_soa<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)n, s->posc, s->velc, s->d_err);
+        NB_CUDA(s, cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream));
+        k_check_soa<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->pos, s->vel, (int)n, s->posc, s->velc, s->d_err,
+                                                                        s->d_mmax);
         NB_CUDA(s, cudaGetLastError());
         rc = check_device_error(s);
         if (rc) { s->n = 0; return rc; }
@@ -996,6 +1025,10 @@ int nb_tune(nb_sim* s, const char* key, int value) {
         } else if (k == "direct_splits") {
             if (value < 0 || value > 4096) return NB_EINVAL;
             s->tune.splits = value;
+        } else if (k == "wait_polls") {
+            if (value < 0 || value > (int)nb::kMaxPolls) return NB_EINVAL;
+            s->wait_polls = (uint32_t)value;
+            return NB_OK;
         } else {
             return NB_EINVAL;
         }
@@ -1013,6 +1046,7 @@ int nb_get_tune(nb_sim* s, const char* key, int* value) {
         if (k == "direct_block") *value = s->tune.block;
         else if (k == "direct_ipt") *value = s->tune.ipt;
         else if (k == "direct_splits") *value = s->tune.splits;
+        else if (k == "wait_polls") *value = (int)s->wait_polls;
         else return NB_EINVAL;
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed

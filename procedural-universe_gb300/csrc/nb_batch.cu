@@ -36,6 +36,8 @@ struct nb_batch {
         int idx = -1;     // slot (Barnes-Hut) or direct-galaxy index
         size_t n_pad = 0;
         const float4* dsrc[4] = {nullptr, nullptr, nullptr, nullptr};   // device source (pos, posc, vel, velc)
+        int gen_model = -1;      // >= 0: generated on the device at commit (nb_batch_add_generated)
+        uint64_t gen_seed = 0;
     };
     std::vector<Gal> gal;
     std::vector<std::vector<float>> h_pos, h_vel;
@@ -70,6 +72,7 @@ struct nb_batch {
     // count here; the wait resizes the tree and runs them again
     int* held = nullptr;
     float pending_dt = 0.f;
+    int steps_not_run = 0;   // of the last launch, when batch_wait gave up (NB_ENOMEM)
     // tuning and graph
     nb_tuning tune{128, 1, 1024, 16, 128};
     cudaGraphExec_t exec = nullptr;
@@ -153,7 +156,7 @@ bool launch_direct_t(nb_batch* b, int grid, cudaStream_t st, float S) {
 #define NB_BD(B, I)                                                                                           \
     if (blk == B && ipt == I) {                                                                               \
         k_batch_direct<LAW, B, I><<<grid, B, 0, st>>>(b->core->pos, b->units, b->unit_comp, b->nunits,         \
-                                                      b->next_unit, S, b->part);                              \
+                                                      b->next_unit, S, b->core->d_mmax, b->part);             \
         return true;                                                                                          \
     }
     NB_BD(64, 1) NB_BD(64, 2) NB_BD(128, 1) NB_BD(128, 2) NB_BD(256, 1)
@@ -171,23 +174,22 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
     const float G = (float)b->base.G;
     TreeBuffers& t = c->tree;
     if (b->n_bh > 0) {
-        NB_BCUDA(b, cudaMemsetAsync(t.interactions, 0, sizeof(unsigned long long), st));
         const int n = (int)b->n_bh;
-        const size_t nk = pad_up((size_t)n, (size_t)tree_sort_tile());
         {
+            // the step's counters, the galaxy cubes, then the forest's keys with the sort's histograms
             PhaseScope ps(c, NB_PHASE_KEYS, 2);
-            k_gal_box_init<<<(6 * b->nslot + 255) / 256, 256, 0, st>>>(b->box_bits, b->nslot);
+            const int words = std::max(6 * b->nslot, tree_counter_words());
+            k_gal_box_init<<<(words + 255) / 256, 256, 0, st>>>(b->box_bits, b->nslot, t.counters,
+                                                               tree_counter_words(), n, t.interactions, b->group_ctr,
+                                                               b->ndgal > 0 ? b->next_unit : nullptr);
             k_gal_box_chunks<<<(unsigned)((n + kBoxChunk - 1) / kBoxChunk), 256, 0, st>>>(c->pos, b->body_slot, n,
                                                                                        b->nslot, b->box_bits);
-            k_gal_box_final<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->box_bits, b->nslot, b->gal_box);
-            k_batch_keys<<<(unsigned)((nk + 255) / 256), 256, 0, st>>>(c->pos, b->body_slot, n, (int)nk, b->gal_box,
-                                                                      t.keys[0], t.vals[0], t.depth);
         }
+        NB_BCUDA(b, tree_batch_keys(c, c->pos, b->body_slot, n, b->box_bits, b->nslot, b->gal_box));
         NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth));
         if (tree_only) return NB_OK;
         {
             PhaseScope ps(c, NB_PHASE_MASS, 3);
-            NB_BCUDA(b, cudaMemsetAsync(t.int_pending, 0, t.int_cap * 4, st));
             k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
                 (int)t.int_cap, t.counters, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
                 t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_walk,
@@ -195,7 +197,6 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
             k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
                                                                  t.int_cell, t.counters, (int)t.int_cap,
                                                                  (int)t.cell_cap, b->gal_root, c->d_err);
-            NB_BCUDA(b, cudaMemsetAsync(b->group_ctr, 0, 2 * sizeof(int), st));
             k_batch_groups<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
                 (int)t.int_cap, t.counters, t.int_cell, b->cell_walk,
                 t.vals[0], b->body_slot, (int)t.cell_cap, n, b->groups, b->group_cap, b->group_ctr, c->d_err);
@@ -216,7 +217,7 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
         b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, b->cell_walk,     \
         b->cell_q1, b->cell_q2, b->gal_box, b->gal_root, b->nslot,                                                \
         (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, (float)(b->far_eta * b->far_eta),   \
-        100.f * S, c->acc, t.interactions, c->d_err)
+        100.f * S, c->d_mmax, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
             else NB_GT(NB_LAW_REFERENCE);
 #undef NB_GT
@@ -225,7 +226,7 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
     }
     if (b->ndgal > 0) {
         PhaseScope ps(c, NB_PHASE_DIRECT_FORCE, 2);
-        NB_BCUDA(b, cudaMemsetAsync(b->next_unit, 0, sizeof(int), st));
+        if (b->n_bh == 0) NB_BCUDA(b, cudaMemsetAsync(b->next_unit, 0, sizeof(int), st));   // else cleared with the counters
         int occ = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_direct<NB_LAW_REFERENCE, 128, 1>,
                                                       b->tune.direct_block, 0);
@@ -416,19 +417,26 @@ int batch_launch_steps(nb_batch* b, float dt, int nsteps) {
 int batch_wait(nb_batch* b) {
     if (!b) return NB_EINVAL;
     cudaSetDevice(b->core->dev);
+    b->steps_not_run = 0;
     for (int attempt = 0;; ++attempt) {
         int rc = nb_synchronize(b->core);
         if (rc) return bfail(b, rc, nb_last_error(b->core));
         int held = 0;
         NB_BCUDA(b, cudaMemcpy(&held, b->held, sizeof(int), cudaMemcpyDeviceToHost));
         if (held == 0) return sync_check(b);
-        if (attempt == 3) return bfail(b, NB_ENOMEM, "the batched octree kept outgrowing its arrays");
+        if (attempt == 3) {
+            // the held steps are the last ones of the launch and left the state as it was
+            b->steps_not_run = held;
+            return bfail(b, NB_ENOMEM, "the batched octree kept outgrowing its arrays");
+        }
         rc = size_tree(b);
         if (rc) return rc;
         rc = batch_launch_steps(b, b->pending_dt, held);
         if (rc) return rc;
     }
 }
+
+int batch_steps_not_run(const nb_batch* b) { return b ? b->steps_not_run : 0; }
 
 }  // namespace nb
 
@@ -506,6 +514,33 @@ int nb_batch_add(nb_batch* b, const float* pos_mass4, const float* vel4, size_t 
     }
 }
 
+int nb_batch_add_generated(nb_batch* b, int model, uint64_t seed, size_t n, int32_t* galaxy) {
+    try {
+        if (!b || n < 2) return NB_EINVAL;
+        if (model < 0 || model > 2) return bfail(b, NB_EINVAL, "unknown galaxy model");
+        if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
+        if (n > kMaxGalaxyBodies) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
+        b->h_pos.emplace_back();
+        b->h_vel.emplace_back();
+        nb_batch::Gal g;
+        g.n = n;
+        g.bh = n >= b->bh_threshold;
+        g.gen_model = model;
+        g.gen_seed = seed;
+        b->gal.push_back(g);
+        if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
+        return NB_OK;
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
+}
+
+int nb_batch_steps_not_run(nb_batch* b, int* steps) {
+    if (!b || !steps) return NB_EINVAL;
+    *steps = b->steps_not_run;
+    return NB_OK;
+}
+
 int nb_batch_commit(nb_batch* b) {
     try {
         if (!b) return NB_EINVAL;
@@ -547,9 +582,12 @@ int nb_batch_commit(nb_batch* b) {
         // galaxies copied in and validated
         int rc = sim_reserve_zeroed(b->core, b->n_total);
         if (rc) return bfail(b, rc, nb_last_error(b->core));
+        std::vector<GenSpec> gen;
         for (size_t k = 0; k < b->gal.size(); ++k) {
             const auto& g = b->gal[k];
-            if (!g.dsrc[0]) {
+            if (g.gen_model >= 0) {
+                gen.push_back(GenSpec{g.gen_seed, g.off, g.n, g.gen_model});
+            } else if (!g.dsrc[0]) {
                 NB_BCUDA(b, cudaMemcpyAsync(b->core->pos + g.off, b->h_pos[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
                                             b->core->stream));
                 NB_BCUDA(b, cudaMemcpyAsync(b->core->vel + g.off, b->h_vel[k].data(), 16 * g.n, cudaMemcpyHostToDevice,
@@ -564,8 +602,27 @@ int nb_batch_commit(nb_batch* b) {
                 for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
             }
         }
+        // galaxies generated on the device, straight into the state arrays
+        NB_BCUDA(b, gen_galaxies(gen, b->core->pos, b->core->vel, b->core->stream));
         rc = sim_check_state(b->core);
         if (rc) return bfail(b, rc, nb_last_error(b->core));
+        if (b->nslot > 0) {
+            // Cell quadrupoles are float sums of m (3 y y - |y|^2): bounded by
+            // 12 M x^2 with M the largest member's mass and x the largest
+            // coordinate.  States beyond float range (the reference's SI-like
+            // masses, 1e20..1e30, at positions of order 1e3) belong to the plain path.
+            unsigned h[2] = {0u, 0u};
+            NB_BCUDA(b, cudaMemcpy(h, b->core->d_mmax, sizeof(h), cudaMemcpyDeviceToHost));
+            float mf, xf;
+            std::memcpy(&mf, &h[0], 4);
+            std::memcpy(&xf, &h[1], 4);
+            size_t nmax = 0;
+            for (const auto& g : b->gal)
+                if (g.bh) nmax = std::max(nmax, g.n);
+            if (12.0 * (double)nmax * (double)mf * (double)xf * (double)xf > 1e37)
+                return bfail(b, NB_ENOTSUP, "Barnes-Hut member beyond the float range of the batched form's cell "
+                                            "quadrupoles (mass x size^2); use N-body units or the plain path");
+        }
         // galaxies handed over from another batch keep their exact state, compensation included
         for (const auto& g : b->gal) {
             if (!g.dsrc[0]) continue;
@@ -855,6 +912,9 @@ int nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4)
             NB_BCUDA(b, cudaMemsetAsync(c->velc + g.off, 0, g.n * 16, c->stream));
             src += g.n;
         }
+        // validated (reported by the next wait) and the largest mass recorded
+        const int rc = sim_rescan_state(c);
+        if (rc) return bfail(b, rc, nb_last_error(c));
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed
         return NB_ENOMEM;

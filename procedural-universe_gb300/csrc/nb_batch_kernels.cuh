@@ -29,11 +29,10 @@
 
 #include <type_traits>
 
+#include "nb_morton.cuh"
+
 namespace nb {
 
-constexpr int kSlotLevels = 7;          // 21 bits of galaxy slot
-constexpr int kMortonLevels = 14;       // 42 bits of position in the galaxy cube
-constexpr int kBatchDepth = kSlotLevels + kMortonLevels;
 constexpr int kGWarps = 4;              // warps per traversal block
 constexpr int kGroupMax = 64;           // bodies per traversal group (two per lane)
 constexpr int kGroupMinDepth = 4;       // a group cell lies >= 4 levels below its galaxy root
@@ -50,18 +49,23 @@ enum : int { BK_SINGLE = 1, BK_BUCKET = 2, BK_INTERNAL = 3 };
 // ---- bounding cube of each Barnes-Hut galaxy ------------------------------
 // Min/max are exact and order-free, so chunks of kBoxChunk bodies reduce in
 // parallel into per-galaxy words with atomics on an order-preserving integer
-// image of the float (total order: -inf < ... < -0 < +0 < ... < +inf).
-__device__ __forceinline__ unsigned float_to_ordered(float f) {
-    const unsigned u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float ordered_to_float(unsigned o) {
-    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
-}
-
-__global__ void k_gal_box_init(unsigned* __restrict__ bits, int nslot) {
+// image of the float (nb_morton.cuh).
+//
+// The first kernel of a batched step also clears the step's counters: the
+// tree counters and the radix histograms (TC_NIN set to the bodies in the
+// forest), the interaction count, the traversal group counters and the
+// direct-sum unit counter.
+__global__ void k_gal_box_init(unsigned* __restrict__ bits, int nslot, int32_t* __restrict__ counters,
+                               int counter_words, int n_in, unsigned long long* __restrict__ interactions,
+                               int* __restrict__ group_ctr, int* __restrict__ next_unit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < 6 * nslot) bits[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
+    for (int j = i; j < counter_words; j += gridDim.x * blockDim.x) counters[j] = j == TC_NIN ? n_in : 0;
+    if (i == 0) {
+        *interactions = 0ull;
+        group_ctr[0] = group_ctr[1] = 0;
+        if (next_unit) *next_unit = 0;
+    }
 }
 
 __device__ __forceinline__ void box_flush(unsigned* bits, int slot, const float lo[3], const float hi[3]) {
@@ -105,50 +109,6 @@ __global__ void __launch_bounds__(256) k_gal_box_chunks(const float4* __restrict
     } else if (cur >= 0) {
         box_flush(bits, cur, lo, hi);
     }
-}
-
-__global__ void k_gal_box_final(const unsigned* __restrict__ bits, int nslot, float4* __restrict__ box) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nslot) return;
-    float lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = ordered_to_float(bits[6 * g + a]);
-        hi[a] = ordered_to_float(bits[6 * g + 3 + a]);
-    }
-    float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-    ext = fmaxf(ext * 1.001f, 1e-20f);
-    box[g] = make_float4(lo[0], lo[1], lo[2], ext);
-}
-
-__device__ __forceinline__ uint64_t spread3(uint32_t v) {   // 14 bits -> every third bit
-    uint64_t x = v & 0x3fffu;
-    x = (x | (x << 16)) & 0x0000ff0000ffull;
-    x = (x | (x << 8)) & 0x00f00f00f00full;
-    x = (x | (x << 4)) & 0x0c30c30c30c3ull;
-    x = (x | (x << 2)) & 0x249249249249ull;
-    return x;
-}
-
-// keys of Barnes-Hut bodies [0, n); pad entries [n, nk) get key ~0.
-__global__ void k_batch_keys(const float4* __restrict__ pos, const int32_t* __restrict__ body_slot, int n, int nk,
-                             const float4* __restrict__ box, uint64_t* __restrict__ keys, int32_t* __restrict__ vals,
-                             int32_t* __restrict__ depth) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nk) return;
-    vals[i] = i;
-    if (i >= n) {
-        keys[i] = ~0ull;
-        return;
-    }
-    const int slot = body_slot[i];
-    const float4 b = box[slot];
-    const float4 p = pos[i];
-    const float sc = 16384.0f / b.w;
-    const uint32_t qx = (uint32_t)min(max((p.x - b.x) * sc, 0.f), 16383.f);
-    const uint32_t qy = (uint32_t)min(max((p.y - b.y) * sc, 0.f), 16383.f);
-    const uint32_t qz = (uint32_t)min(max((p.z - b.z) * sc, 0.f), 16383.f);
-    keys[i] = ((uint64_t)slot << (3 * kMortonLevels)) | spread3(qx) | (spread3(qy) << 1) | (spread3(qz) << 2);
-    depth[i] = kBatchDepth;
 }
 
 // ---- bottom-up mass, centre of mass and quadrupole --------------------------
@@ -397,7 +357,7 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ counters
 template <int LAW>
 __device__ __forceinline__ void cell_pair_accel(float2 cx, float2 cy, float2 cz, float2 cm, float2 qxx, float2 qyy,
                                                 float2 qzz, float2 qxy, float2 qxz, float2 qyz, float2 nx, float2 ny,
-                                                float2 nz, float2 S2, float2& ax, float2& ay, float2& az) {
+                                                float2 nz, float2 S2, float2 T2, float2& ax, float2& ay, float2& az) {
     const float2 dx = __fadd2_rn(cx, nx);
     const float2 dy = __fadd2_rn(cy, ny);
     const float2 dz = __fadd2_rn(cz, nz);
@@ -407,7 +367,7 @@ __device__ __forceinline__ void cell_pair_accel(float2 cx, float2 cy, float2 cz,
     float2 w, ir;
     if (LAW == NB_LAW_REFERENCE) {
         const float2 s = __fadd2_rn(r2, S2);
-        const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, make_float2(kTiny, kTiny));
+        const float2 t = __ffma2_rn(__fmul2_rn(r2, s), s, T2);
         const float2 rt = make_float2(rsqrt_approx(t.x), rsqrt_approx(t.y));
         w = __fmul2_rn(cm, rt);
         ir = __fmul2_rn(rt, s);
@@ -538,7 +498,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const int4* __restrict__ cell_walk, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
     const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
     int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_min_r2,
-    float4* __restrict__ acc,
+    const unsigned* __restrict__ mmax, float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
     __shared__ float4 lcl[kGWarps][kGCells / 2][5];
@@ -549,6 +509,8 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const uint32_t lt = (1u << lane) - 1u;
     const int ngroups = min(*n_groups_dev, group_cap);
     const float2 S2 = make_float2(S, S);
+    const float tiny = self_pair_tiny(mmax);   // a leaf's bodies include the target itself
+    const float2 T2 = make_float2(tiny, tiny);
     unsigned long long total = 0;
     for (;;) {
     int gi = 0;
@@ -614,9 +576,11 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
                 const float2 cm = make_float2(e1.z, e1.w), qxx = make_float2(e2.x, e2.y), qyy = make_float2(e2.z, e2.w);
                 const float2 qzz = make_float2(e3.x, e3.y), qxy = make_float2(e3.z, e3.w), qxz = make_float2(e4.x, e4.y);
                 const float2 qyz = make_float2(e4.z, e4.w);
-                cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n0x, n0y, n0z, S2, a0x, a0y, a0z);
+                cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n0x, n0y, n0z, S2, T2, a0x, a0y,
+                                     a0z);
                 if (decltype(both)::value)
-                    cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+                    cell_pair_accel<LAW>(cx, cy, cz, cm, qxx, qyy, qzz, qxy, qxz, qyz, n1x, n1y, n1z, S2, T2, a1x, a1y,
+                                         a1z);
             }
         };
         if (dual) cell_loop(std::true_type{}); else cell_loop(std::false_type{});
@@ -640,16 +604,17 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
                     const float4 e0 = lbd[w][k + u][0], e1 = lbd[w][k + u][1];
                     const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
                     const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
-                    interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
-                    if (decltype(both)::value) interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+                    interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, T2, a0x, a0y, a0z);
+                    if (decltype(both)::value)
+                        interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, T2, a1x, a1y, a1z);
                 }
             }
             for (; k < np; ++k) {
                 const float4 e0 = lbd[w][k][0], e1 = lbd[w][k][1];
                 const float2 bx = make_float2(e0.x, e0.y), by = make_float2(e0.z, e0.w);
                 const float2 bz = make_float2(e1.x, e1.y), bm = make_float2(e1.z, e1.w);
-                interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, a0x, a0y, a0z);
-                if (decltype(both)::value) interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, a1x, a1y, a1z);
+                interact_x2<LAW>(bx, by, bz, bm, n0x, n0y, n0z, S2, T2, a0x, a0y, a0z);
+                if (decltype(both)::value) interact_x2<LAW>(bx, by, bz, bm, n1x, n1y, n1z, S2, T2, a1x, a1y, a1z);
             }
         };
         if (dual) body_loop(std::true_type{}); else body_loop(std::false_type{});
@@ -834,8 +799,10 @@ template <int LAW, int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK) k_batch_direct(const float4* __restrict__ pos, const int4* __restrict__ units,
                                                         const int32_t* __restrict__ unit_comp, int nunits,
                                                         int* __restrict__ next_unit, float S,
+                                                        const unsigned* __restrict__ mmax,
                                                         float4* __restrict__ part) {
     __shared__ float4 tile[kDirTile];
+    const float tiny = self_pair_tiny(mmax);
     __shared__ int cur;
     static_assert(kDirTile % BLOCK == 0 || BLOCK % kDirTile == 0, "tile/block");
     while (true) {
@@ -865,7 +832,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch_direct(const float4* __restrict
                 for (int j = 0; j < kFold; ++j) {
                     const float4 pj = tile[f + j];
 #pragma unroll
-                    for (int k = 0; k < IPT; ++k) interact<LAW>(pj, xi[k], yi[k], zi[k], S, tx[k], ty[k], tz[k]);
+                    for (int k = 0; k < IPT; ++k)
+                        interact<LAW>(pj, xi[k], yi[k], zi[k], S, tiny, tx[k], ty[k], tz[k]);
                 }
 #pragma unroll
                 for (int k = 0; k < IPT; ++k) {

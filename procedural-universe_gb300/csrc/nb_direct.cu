@@ -32,12 +32,17 @@
 namespace nb {
 
 // K1: grid (target blocks, source ranges). Writes part[split][i] (sum) and
-// part[splits + split][i] (compensation).
+// part[splits + split][i] (compensation).  polls bounds each wait for a
+// source tile (kMaxPolls normally; smaller only to test the timeout path);
+// the copies still in flight after a wait gave up are always waited for with
+// the full budget before the block exits.
 template <int LAW, int BLOCK, int IPT, bool COMP>
 __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict__ pos, int n_pad,
                                                         int tiles_per_split, int ntiles, int splits, float S,
-                                                        float4* __restrict__ part, int* __restrict__ err) {
+                                                        float4* __restrict__ part, int* __restrict__ err,
+                                                        uint32_t polls, const unsigned* __restrict__ mmax) {
     __shared__ __align__(128) float4 tile[2][kTileJ];
+    const float tiny = self_pair_tiny(mmax);
     __shared__ __align__(8) uint64_t bar[2];
 
     const int split = blockIdx.y;
@@ -74,7 +79,7 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
     bool abandoned = false;
     for (; t < nt; ++t) {
         const int b = t & 1;
-        const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((t >> 1) & 1));
+        const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((t >> 1) & 1), polls);
         const float4* tj = tile[b];
 #pragma unroll 1
         for (int f = 0; f < kTileJ; f += kFold) {
@@ -85,7 +90,7 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
                 float2 ax[P], ay[P], az[P];
 #pragma unroll
                 for (int k = 0; k < P; ++k) ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
-                const float2 S2 = make_float2(S, S);
+                const float2 S2 = make_float2(S, S), T2 = make_float2(tiny, tiny);
 #pragma unroll 4
                 for (int j = 0; j < kFold; ++j) {
                     const float4 pj = tj[f + j];
@@ -95,7 +100,7 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
                     for (int k = 0; k < P; ++k)
                         interact_x2<LAW>(jx, jy, jz, jm, make_float2(-xi[2 * k], -xi[2 * k + 1]),
                                          make_float2(-yi[2 * k], -yi[2 * k + 1]), make_float2(-zi[2 * k], -zi[2 * k + 1]),
-                                         S2, ax[k], ay[k], az[k]);
+                                         S2, T2, ax[k], ay[k], az[k]);
                 }
 #pragma unroll
                 for (int k = 0; k < P; ++k) {
@@ -110,7 +115,8 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
                 for (int j = 0; j < kFold; ++j) {
                     const float4 pj = tj[f + j];
 #pragma unroll
-                    for (int k = 0; k < IPT; ++k) interact<LAW>(pj, xi[k], yi[k], zi[k], S, tx[k], ty[k], tz[k]);
+                    for (int k = 0; k < IPT; ++k)
+                        interact<LAW>(pj, xi[k], yi[k], zi[k], S, tiny, tx[k], ty[k], tz[k]);
                 }
             }
 #pragma unroll
@@ -136,7 +142,8 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
         // Let the copies still in flight land before the block's shared
         // memory is released (bounded), then report.
         if (threadIdx.x == 0) {
-            for (int q = t; q < nt && q < t + 2; ++q) (void)mbar_wait_bounded(&bar[q & 1], (uint32_t)((q >> 1) & 1));
+            for (int q = t; q < nt && q < t + 2; ++q)
+                (void)mbar_wait_bounded(&bar[q & 1], (uint32_t)((q >> 1) & 1), kMaxPolls);
             record_error(err, DEV_WAIT_TIMEOUT);
         }
         return;
@@ -154,7 +161,9 @@ __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict
 // K7: fold the partials of all source ranges (fixed order), apply G, add the
 // pending initial forces, store the acceleration and, when update != 0,
 // kick-drift: v += a dt; x += v dt / scale, both Kahan-compensated
-// (src/Sim/BruteForceCPU.cpp:61-73).
+// (src/Sim/BruteForceCPU.cpp:61-73).  When the error word is set (a force
+// block abandoned a wait, or an earlier error has not been read yet) the
+// step is abandoned: acceleration and state stay as they were.
 // Render hand-off in the update's epilogue: the vertex (LWParticle layout,
 // 32 bytes) of a body the update just moved, as two 16-byte stores.
 __device__ __forceinline__ void write_vertex(nb_render_vertex* rv, const float4* rcol, float rscale, int i,
@@ -170,9 +179,10 @@ __global__ void k_direct_reduce_update(const float4* __restrict__ part, int spli
                                        float4* __restrict__ pos, float4* __restrict__ posc,
                                        float4* __restrict__ vel, float4* __restrict__ velc, float dt,
                                        float inv_scale, int update, int comp, nb_render_vertex* __restrict__ rv,
-                                       const float4* __restrict__ rcol, float rscale) {
+                                       const float4* __restrict__ rcol, float rscale,
+                                       const int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || *err != 0) return;
     float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
     for (int s = 0; s < splits; ++s) {
         const float4 p = part[(size_t)s * n_pad + i];
@@ -245,17 +255,19 @@ namespace {
 
 template <int LAW, int BLOCK, int IPT, bool COMP>
 void launch_force_t(dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps, int ntiles, int splits,
-                    float S, float4* part, int* err) {
-    k_direct_force<LAW, BLOCK, IPT, COMP><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S, part, err);
+                    float S, float4* part, int* err, uint32_t polls, const unsigned* mmax) {
+    k_direct_force<LAW, BLOCK, IPT, COMP><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S, part, err,
+                                                                 polls, mmax);
 }
 
 template <int LAW, bool COMP>
 bool launch_force_law(int block, int ipt, dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps,
-                      int ntiles, int splits, float S, float4* part, int* err) {
-#define NB_CASE(B, I)                                                                      \
-    if (block == B && ipt == I) {                                                          \
-        launch_force_t<LAW, B, I, COMP>(grid, st, pos, n_pad, tps, ntiles, splits, S, part, err); \
-        return true;                                                                       \
+                      int ntiles, int splits, float S, float4* part, int* err, uint32_t polls,
+                      const unsigned* mmax) {
+#define NB_CASE(B, I)                                                                                    \
+    if (block == B && ipt == I) {                                                                        \
+        launch_force_t<LAW, B, I, COMP>(grid, st, pos, n_pad, tps, ntiles, splits, S, part, err, polls, mmax); \
+        return true;                                                                                     \
     }
     NB_CASE(64, 1) NB_CASE(64, 2) NB_CASE(64, 4) NB_CASE(64, 8)
     NB_CASE(128, 1) NB_CASE(128, 2) NB_CASE(128, 4) NB_CASE(128, 8)
@@ -323,17 +335,17 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     if (sim->prm.law == NB_LAW_PLUMMER)
         ok = comp ? launch_force_law<NB_LAW_PLUMMER, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                           (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                          sim->d_err)
+                                                          sim->d_err, sim->wait_polls, sim->d_mmax)
                   : launch_force_law<NB_LAW_PLUMMER, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                            (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                           sim->d_err);
+                                                           sim->d_err, sim->wait_polls, sim->d_mmax);
     else
         ok = comp ? launch_force_law<NB_LAW_REFERENCE, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                             (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                            sim->d_err)
+                                                            sim->d_err, sim->wait_polls, sim->d_mmax)
                   : launch_force_law<NB_LAW_REFERENCE, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                              (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                             sim->d_err);
+                                                             sim->d_err, sim->wait_polls, sim->d_mmax);
     }
     if (!ok) return cudaErrorInvalidConfiguration;
     cudaError_t e = cudaGetLastError();
@@ -344,7 +356,7 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     k_direct_reduce_update<<<(n + 255) / 256, 256, 0, sim->stream>>>(
         sim->part, splits, n, (int)sim->n_pad, (float)sim->prm.G, sim->finit_pending ? sim->finit : nullptr,
         sim->acc, sim->pos, sim->posc, sim->vel, sim->velc, dt, inv_scale, update ? 1 : 0, comp ? 1 : 0,
-        update ? sim->render : nullptr, sim->rcolour, sim->rscale);
+        update ? sim->render : nullptr, sim->rcolour, sim->rscale, sim->d_err);
     sim->finit_pending = false;
     const double nn = (double)sim->n;
     sim->inter_last = (uint64_t)(nn * (nn - 1.0));
@@ -384,13 +396,21 @@ constexpr int kNoAllocMaxSplits = 8;
 constexpr size_t kNoAllocScratch = (size_t)NB_NOALLOC_MAX_BODIES * (1 + 2 * kNoAllocMaxSplits);
 static __device__ __align__(256) float4 g_noalloc_scratch[kNoAllocScratch];   // 17.8 MB
 static __device__ int g_noalloc_err;
+// float bits of the call's largest |mass| (the force law's self-pair guard);
+// zero between calls: the reduce kernel clears it after the force kernel read it
+static __device__ unsigned g_noalloc_mmax;
 
 // Copies n bodies into the scratch and zero-fills the padding (zero-mass
-// bodies at the origin contribute exactly nothing); clears the error word.
+// bodies at the origin contribute exactly nothing); clears the error word and
+// records the largest |mass|.
 __global__ void k_noalloc_stage(const float4* __restrict__ in, int n, int n_pad, float4* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) g_noalloc_err = 0;
-    if (i < n_pad) out[i] = i < n ? in[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n_pad) {
+        const float4 p = i < n ? in[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        out[i] = p;
+        if (i < n) atomicMax(&g_noalloc_mmax, __float_as_uint(fabsf(p.w)));
+    }
 }
 
 // Folds the partials like k_direct_reduce_update; a force kernel whose bounded
@@ -411,12 +431,14 @@ __global__ void k_noalloc_reduce(const float4* __restrict__ part, int splits, in
     float4 a = make_float4(G * (ax - (kx + qx)), G * (ay - (ky + qy)), G * (az - (kz + qz)), 0.f);
     if (g_noalloc_err != 0) a = make_float4(NAN, NAN, NAN, NAN);
     acc[i] = a;
+    if (i == 0) g_noalloc_mmax = 0u;
 }
 
 namespace {
 std::mutex g_noalloc_mu;
 float4* g_noalloc_ptr[256] = {};   // device address of the scratch, per device ordinal
 int* g_noalloc_err_ptr[256] = {};
+unsigned* g_noalloc_mmax_ptr[256] = {};
 }  // namespace
 
 }  // namespace nb
@@ -435,22 +457,27 @@ extern "C" int nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* 
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) { cudaGetLastError(); return NB_ECUDA; }
     float4* scratch = nullptr;
     int* err = nullptr;
+    unsigned* mmax = nullptr;
     {
         // Set-up on the first call on each device, with that device current.
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
         if (!g_noalloc_ptr[dev]) {
             void* p = nullptr;
             void* q = nullptr;
+            void* r = nullptr;
             if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess ||
-                cudaGetSymbolAddress(&q, g_noalloc_err) != cudaSuccess || !p || !q) {
+                cudaGetSymbolAddress(&q, g_noalloc_err) != cudaSuccess ||
+                cudaGetSymbolAddress(&r, g_noalloc_mmax) != cudaSuccess || !p || !q || !r) {
                 cudaGetLastError();
                 return NB_ECUDA;
             }
             g_noalloc_ptr[dev] = static_cast<float4*>(p);
             g_noalloc_err_ptr[dev] = static_cast<int*>(q);
+            g_noalloc_mmax_ptr[dev] = static_cast<unsigned*>(r);
         }
         scratch = g_noalloc_ptr[dev];
         err = g_noalloc_err_ptr[dev];
+        mmax = g_noalloc_mmax_ptr[dev];
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t n_pad = pad_up(n, kPad);
@@ -467,9 +494,9 @@ extern "C" int nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* 
     const float S = (float)softening2;
     bool ok = law == NB_LAW_PLUMMER
                   ? launch_force_law<NB_LAW_PLUMMER, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles, splits,
-                                                          S, part, err)
+                                                          S, part, err, kMaxPolls, mmax)
                   : launch_force_law<NB_LAW_REFERENCE, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles,
-                                                            splits, S, part, err);
+                                                            splits, S, part, err, kMaxPolls, mmax);
     if (!ok) return NB_EINVAL;
     k_noalloc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)n, (int)n_pad, (float)G,
                                                                  reinterpret_cast<float4*>(accel4));

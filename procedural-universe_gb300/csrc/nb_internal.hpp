@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 #include "../../include/nbody_gb300.h"
+#include "nb_common.cuh"
 
 namespace nb {
 
@@ -35,8 +36,6 @@ struct TreeBuffers {
     size_t int_cap = 0;    // internal nodes
     size_t cell_cap = 0;   // cells
     size_t hash_cap = 0;   // power of two
-    size_t scan_cap = 0;   // scan block-sum entries
-    size_t hist_cap = 0;   // radix histogram entries
     // per body
     uint64_t* keys[2] = {nullptr, nullptr};  // radix ping-pong (input order in [0] before the sort)
     int32_t* vals[2] = {nullptr, nullptr};   // original index per sorted position
@@ -68,12 +67,14 @@ struct TreeBuffers {
     // internal node lookup by code
     uint64_t* hkeys = nullptr;
     int32_t* hvals = nullptr;
-    // radix sort
-    int32_t* hist = nullptr;                 // [digit][tile]
-    uint32_t* ghist = nullptr;               // [pass][digit]
+    // radix sort and the single-pass scans (decoupled look-back)
+    uint32_t* ghist = nullptr;               // [pass][digit], inside the counters buffer
     int32_t* plan = nullptr;                 // [0..7] skip, [8..15] source buffer, [16] final buffer
-    int32_t* scan_sums = nullptr;
-    // counters (device) and their pinned host mirror
+    int32_t* dig_off = nullptr;              // [pass][digit]: where the digit's keys start
+    unsigned long long* sort_status = nullptr;   // [pass][tile][digit]
+    unsigned long long* pos_status = nullptr;    // [tile]: positions scan (body_cap / sort tile)
+    unsigned long long* popc_status = nullptr;   // [tile]: child-count scan (int_cap / sort tile)
+    // counters (device: kCounterWords words, then ghist) and their pinned host mirror
     int32_t* counters = nullptr;
     int32_t* h_counters = nullptr;
     unsigned long long* interactions = nullptr;
@@ -91,8 +92,13 @@ enum : int {
     TC_DEEPER = 4,    // depth-cap buckets whose bodies differ (the reference would split further)
     TC_HASHFAIL = 5,  // failed internal-node lookups (must stay 0)
     TC_OVERFLOW = 6,  // nodes beyond the allocated capacity (must stay 0)
-    TC_COUNT = 8
+    TC_COUNT = 8,     // the counters above are read by the host
+    // tile counters of the look-back kernels (blocks take tiles in start order)
+    TC_TILE_POS = 8,
+    TC_TILE_POPC = 9,
+    TC_TILE_SORT = 10,   // one per radix pass
 };
+constexpr int kCounterWords = 32;   // counters before the radix histograms in the same buffer
 
 #ifdef __CUDACC__
 // Whether a tree built over fixed capacities (int_cap internal nodes,
@@ -165,12 +171,19 @@ struct nb_sim {
     double* dscratch = nullptr;
     size_t dscratch_cap = 0;
     int* d_err = nullptr;     // device error word
+    // float bits of the state's largest |mass| (the direct sum's self-pair
+    // guard) and of its largest |coordinate|, recorded when a state is loaded
+    unsigned* d_mmax = nullptr;
     int* h_err = nullptr;     // pinned: [0] mirror of d_err, [1] init's non-zero-force flag
     unsigned long long* d_inter = nullptr;
     uint64_t inter_last = 0;
     bool forces_fresh = false;  // acc holds the forces of the current positions
     nb::Profiler prof{};
     bool tune_set = false;     // direct-sum tuning set through nb_tune (else sized by n)
+    // polls of each source-tile wait of the direct-sum force kernel before the
+    // step is abandoned (nb_tune "wait_polls"; lowered only by the test of the
+    // timeout path)
+    uint32_t wait_polls = nb::kMaxPolls;
     std::string err;
 };
 
@@ -204,6 +217,13 @@ cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal);
 float theta_float(double theta);   // smallest float >= theta
 // Batched form: topology of pre-computed keys without host synchronisation.
 cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D);
+// Words of the counters buffer (counters, tile counters, radix histograms)
+// that a batched step clears before its keys.
+int tree_counter_words();
+// Keys of the batched forest with the sort's histograms; writes each
+// galaxy's cube (x0, y0, z0, edge) from its ordered min/max words.
+cudaError_t tree_batch_keys(nb_sim* sim, const float4* pos, const int32_t* body_slot, int n,
+                            const unsigned* box_bits, int nslot, float4* gal_box);
 cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells);
 int tree_sort_tile();
 
@@ -212,8 +232,11 @@ int tree_sort_tile();
 // origin), for the caller to fill by copies on sim->stream.
 int sim_reserve_zeroed(nb_sim* s, size_t n);
 // Validates positions and velocities (finite) and zeroes the compensation
-// arrays, as nb_init_soa does after its upload.
+// arrays, as nb_init_soa does after its upload; records the largest mass.
 int sim_check_state(nb_sim* s);
+// The same without waiting: a non-finite value is reported by the next
+// synchronisation.
+int sim_rescan_state(nb_sim* s);
 
 // ---- batched form hand-over (nb_batch.cu), used by the served form ----
 constexpr size_t kMaxGalaxyBodies = (size_t)1 << 24;   // bodies of one galaxy in the batched form
@@ -225,6 +248,20 @@ int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const fl
 // the device's error and overflow flags.
 int batch_launch_steps(nb_batch* b, float dt, int nsteps);
 int batch_wait(nb_batch* b);
+// Steps of the last launch that were not run when batch_wait failed with
+// NB_ENOMEM (the octree kept outgrowing its arrays); 0 otherwise.
+int batch_steps_not_run(const nb_batch* b);
+
+// ---- galaxies generated on the device (nb_gen.cu) ----
+// model: 0 exponential disk + 10% Hernquist bulge, 1 Plummer sphere, 2 two
+// Plummer spheres on a parabolic orbit (the host generators' defaults).
+struct GenSpec {
+    uint64_t seed;
+    size_t off;   // first body in the state arrays
+    size_t n;
+    int model;
+};
+cudaError_t gen_galaxies(const std::vector<GenSpec>& specs, float4* pos, float4* vel, cudaStream_t st);
 
 // ---- profiling (nb_api.cu) ----
 // Records CUDA events around one phase on sim->stream when profiling is on

@@ -6,15 +6,14 @@
 // free and the estimated device bytes of the active jobs stay within the
 // budget.  When the active set changes, a new batch is built from the active
 // jobs -- continuing jobs hand their state over device to device, new jobs
-// bring freshly generated initial conditions -- and the active jobs are
-// stepped together by the batched form for up to steps_per_round steps,
-// never past the nearest completion and, when round_seconds is set, for no
-// more steps than fit in round_seconds at the batch's measured time per step
-// (the first round of a new batch takes one step to measure it), so that jobs
-// arriving meanwhile are admitted soon.  While a round runs on the device the
-// host generates the initial conditions of the queued jobs that the next
-// admission can take.  Every job's state stays on the device from admission
-// to completion.
+// have their initial conditions generated on the device, straight into the
+// batch's arrays (nb_gen.cu) -- and the active jobs are stepped together by
+// the batched form for up to steps_per_round steps, never past the nearest
+// completion and, when round_seconds is set, for no more steps than fit in
+// round_seconds at the batch's measured time per step (the first round of a
+// new batch takes one step to measure it), so that jobs arriving meanwhile
+// are admitted soon.  Every job's state stays on the device from admission to
+// completion; nothing of a job is made on the host.
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
 #include <chrono>
@@ -41,8 +40,7 @@ struct Job {
     nb_job spec{};
     nb_job_status st{};
     int galaxy = -1;                // index in the current batch
-    bool generated = false;         // init_pos / init_vel hold its initial conditions
-    std::vector<float> init_pos, init_vel, res_pos, res_vel;
+    std::vector<float> res_pos, res_vel;
 };
 
 }  // namespace
@@ -63,7 +61,7 @@ struct nb_server {
     double step_s = 0;              // measured seconds per step of the current batch (0: not yet)
     uint64_t body_steps = 0, rounds = 0;
     uint64_t rebuilds = 0, batch_steps = 0, step_launches = 0;   // where the time went
-    double rebuild_s = 0, stepping_s = 0, generate_s = 0;
+    double rebuild_s = 0, stepping_s = 0;
 };
 
 namespace {
@@ -79,22 +77,10 @@ double now_s(const nb_server* s) {
 
 size_t job_bytes(const nb_job& j) { return j.n * kBytesPerBody; }
 
-int generate(Job& j) {
-    if (j.generated) return NB_OK;
-    const size_t n = j.spec.n;
-    j.init_pos.assign(4 * n, 0.f);
-    j.init_vel.assign(4 * n, 0.f);
-    const int rc = j.spec.model == 1
-                       ? nb_seed_plummer(j.spec.seed, n, 1.0, 1.0, j.init_pos.data(), j.init_vel.data())
-                       : nb_seed_disk(j.spec.seed, n, 1.0, 1.0, 0.1, 0.1, 0.2, 0.05, j.init_pos.data(),
-                                      j.init_vel.data());
-    j.generated = rc == NB_OK;
-    return rc;
-}
-
 // Builds a batch of the active jobs; continuing jobs take their state from
-// the previous batch (device to device).  On failure the previous batch and
-// the jobs' places in it are left as they were.
+// the previous batch (device to device), new jobs are generated on the device
+// at commit.  On failure the previous batch and the jobs' places in it are
+// left as they were.
 int rebuild(nb_server* s) {
     nb_batch* nb2 = nullptr;
     int rc = nb_batch_create(&s->prm.base, s->prm.bh_threshold, s->prm.base.theta, &nb2);
@@ -109,7 +95,7 @@ int rebuild(nb_server* s) {
             rc = batch_device_state(s->batch, j.galaxy, &p, &pc, &v, &vc, &n);
             if (!rc) rc = batch_add_device(nb2, p, pc, v, vc, n, &g);
         } else {
-            rc = nb_batch_add(nb2, j.init_pos.data(), j.init_vel.data(), j.spec.n, &g);
+            rc = nb_batch_add_generated(nb2, j.spec.model, j.spec.seed, j.spec.n, &g);
         }
         if (rc) {
             std::string m = nb_batch_last_error(nb2);
@@ -127,15 +113,7 @@ int rebuild(nb_server* s) {
     if (s->batch) nb_batch_destroy(s->batch);
     s->batch = nb2;
     s->step_s = 0;
-    for (size_t a = 0; a < s->active.size(); ++a) {
-        Job& j = s->jobs[s->active[a]];
-        j.galaxy = place[a];
-        j.init_pos.clear();
-        j.init_pos.shrink_to_fit();
-        j.init_vel.clear();
-        j.init_vel.shrink_to_fit();
-        j.generated = false;
-    }
+    for (size_t a = 0; a < s->active.size(); ++a) s->jobs[s->active[a]].galaxy = place[a];
     return NB_OK;
 }
 
@@ -253,10 +231,6 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
             if (s->bytes_used + j.st.bytes > s->prm.memory_budget) break;
             if (s->bodies_used + j.spec.n > kMaxBatchBodies) break;
             if (!std::isnan(s->dt) && j.spec.dt != s->dt) break;   // waits for a round with its dt
-            const double t_gen = now_s(s);
-            int rc = generate(j);
-            s->generate_s += now_s(s) - t_gen;
-            if (rc) return sfail(s, rc, "job generation failed");
             j.st.state = 1;
             j.st.admit_s = now_s(s);
             j.galaxy = -1;
@@ -297,38 +271,21 @@ int nb_server_tick(nb_server* s, int* active, int* queued) {
             nb_batch_launch_count(s->batch, &l1);
             s->step_launches += l1 - l0;
             if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
-            // meanwhile: initial conditions of the queued jobs the next admission can take
-            bool generated = false;
-            {
-                int slots = s->prm.max_active - (int)s->active.size();
-                size_t bytes = s->bytes_used, bodies = s->bodies_used;
-                for (uint64_t id : s->queue) {
-                    Job& j = s->jobs[id];
-                    if (slots <= 0 || bytes + j.st.bytes > s->prm.memory_budget) break;
-                    if (bodies + j.spec.n > kMaxBatchBodies || j.spec.dt != s->dt) break;
-                    generated |= !j.generated;
-                    const double t_gen = now_s(s);
-                    rc = generate(j);
-                    s->generate_s += now_s(s) - t_gen;
-                    if (rc) break;   // reported when the job is admitted
-                    --slots;
-                    bytes += j.st.bytes;
-                    bodies += j.spec.n;
-                }
-            }
             rc = batch_wait(s->batch);
-            if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
-            // a round that also generated may have outlasted its steps: keep the last clean figure
+            // a round the batch could not finish (its octree kept outgrowing its
+            // arrays) ran its first k - not_run steps: the jobs' counts follow
+            const int ran = rc ? k - batch_steps_not_run(s->batch) : k;
             const double t_end = now_s(s);
-            if (!generated || s->step_s == 0) s->step_s = (t_end - t_round) / k;
+            if (!rc) s->step_s = (t_end - t_round) / k;
             s->stepping_s += t_end - t_round;
-            s->batch_steps += (uint64_t)k;
+            s->batch_steps += (uint64_t)ran;
             for (uint64_t id : s->active) {
                 Job& j = s->jobs[id];
-                j.st.steps_done += k;
-                s->body_steps += (uint64_t)k * j.spec.n;
+                j.st.steps_done += ran;
+                s->body_steps += (uint64_t)ran * j.spec.n;
             }
             ++s->rounds;
+            if (rc) return sfail(s, rc, std::string("step: ") + nb_batch_last_error(s->batch));
         }
         if (active) *active = (int)s->active.size();
         if (queued) *queued = (int)s->queue.size();
@@ -388,7 +345,7 @@ int nb_server_timing(nb_server* s, uint64_t* rebuilds, double* rebuild_s, uint64
         if (rebuild_s) *rebuild_s = s->rebuild_s;
         if (batch_steps) *batch_steps = s->batch_steps;
         if (step_s) *step_s = s->stepping_s;
-        if (generate_s) *generate_s = s->generate_s;
+        if (generate_s) *generate_s = 0.0;   // initial conditions are made on the device, inside rebuild_s
         if (step_launches) *step_launches = s->step_launches;
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed

@@ -12,8 +12,10 @@
 //    with the half-open containment of BoundingCube::Contains
 //    (src/Sim/Octree.hpp:18-22).  A body outside the root cube gets key ~0:
 //    the reference drops it from the tree but counts it in the root.
-//  * K3: stable LSD radix sort of (key, body) pairs, 8 passes of 8 bits
-//    (reduce-then-scan; the scatter ranks digits with warp match_any).
+//  * K3: stable LSD radix sort of (key, body) pairs, 8 passes of 8 bits, one
+//    launch per pass: the digit histograms of all passes come with the keys,
+//    and each pass ranks, finds its tile's offsets by decoupled look-back and
+//    scatters in one kernel (the scatter ranks digits with warp match_any).
 //    Passes whose digit is the same for every key are skipped on the device.
 //  * K4: the reference tree splits a node when a second body arrives and
 //    creates all 8 children, so its internal nodes are exactly the key
@@ -36,6 +38,8 @@
 #include "nb_common.cuh"
 #include "nb_internal.hpp"
 #include "nb_scan.cuh"
+#include "nb_lookback.cuh"
+#include "nb_morton.cuh"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -58,72 +62,55 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 // ---------------------------------------------------------------- K2 keys --
-__global__ void k_keys(const float4* __restrict__ pos, int n, int nk, float half, int D,
-                       uint64_t* __restrict__ keys, int32_t* __restrict__ vals, int32_t* __restrict__ depth,
-                       int32_t* __restrict__ counters) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nk) return;
-    vals[i] = i;
-    bool inside = false, gap = false;
-    if (i < n) {
-        const float4 p = pos[i];
-        float lo0 = -half, lo1 = -half, lo2 = -half, hi0 = half, hi1 = half, hi2 = half;
-        inside = p.x >= lo0 && p.y >= lo1 && p.z >= lo2 && p.x < hi0 && p.y < hi1 && p.z < hi2;
-        uint64_t key = ~0ull;
-        int d = 0;
-        if (inside) {
-            key = 0;
-            float size = __fsub_rn(hi0, lo0);
-            for (int l = 0; l < D; ++l) {
-                const float s = __fdiv_rn(size, 2.0f);
-                const float m0 = __fadd_rn(lo0, s), m1 = __fadd_rn(lo1, s), m2 = __fadd_rn(lo2, s);
-                const float t0 = __fadd_rn(m0, s), t1 = __fadd_rn(m1, s), t2 = __fadd_rn(m2, s);
-                int oct = 0;
-                bool ok = true;
-                if (p.x >= m0 && p.x < t0) { oct |= 1; lo0 = m0; hi0 = t0; }
-                else if (p.x >= lo0 && p.x < m0) { hi0 = m0; }
-                else ok = false;
-                if (p.y >= m1 && p.y < t1) { oct |= 2; lo1 = m1; hi1 = t1; }
-                else if (p.y >= lo1 && p.y < m1) { hi1 = m1; }
-                else ok = false;
-                if (p.z >= m2 && p.z < t2) { oct |= 4; lo2 = m2; hi2 = t2; }
-                else if (p.z >= lo2 && p.z < m2) { hi2 = m2; }
-                else ok = false;
-                if (!ok) break;
-                size = __fsub_rn(hi0, lo0);
-                key = (key << 3) | (uint64_t)oct;
-                ++d;
-            }
-            if (d < D) {   // a gap between float child bounds: left-align the path
-                key <<= 3 * (D - d);
-                gap = true;
-            }
-        }
-        keys[i] = key;
-        depth[i] = d;
-    } else {
-        keys[i] = ~0ull;
+// The octant path of body p (Octree::Add's descent) and its length; gap: the
+// path met a gap between float child bounds and was cut short.
+__device__ __forceinline__ uint64_t body_key(const float4 p, float half, int D, bool& inside, bool& gap, int& d) {
+    float lo0 = -half, lo1 = -half, lo2 = -half, hi0 = half, hi1 = half, hi2 = half;
+    inside = p.x >= lo0 && p.y >= lo1 && p.z >= lo2 && p.x < hi0 && p.y < hi1 && p.z < hi2;
+    gap = false;
+    d = 0;
+    if (!inside) return ~0ull;
+    uint64_t key = 0;
+    float size = __fsub_rn(hi0, lo0);
+    for (int l = 0; l < D; ++l) {
+        const float s = __fdiv_rn(size, 2.0f);
+        const float m0 = __fadd_rn(lo0, s), m1 = __fadd_rn(lo1, s), m2 = __fadd_rn(lo2, s);
+        const float t0 = __fadd_rn(m0, s), t1 = __fadd_rn(m1, s), t2 = __fadd_rn(m2, s);
+        int oct = 0;
+        bool ok = true;
+        if (p.x >= m0 && p.x < t0) { oct |= 1; lo0 = m0; hi0 = t0; }
+        else if (p.x >= lo0 && p.x < m0) { hi0 = m0; }
+        else ok = false;
+        if (p.y >= m1 && p.y < t1) { oct |= 2; lo1 = m1; hi1 = t1; }
+        else if (p.y >= lo1 && p.y < m1) { hi1 = m1; }
+        else ok = false;
+        if (p.z >= m2 && p.z < t2) { oct |= 4; lo2 = m2; hi2 = t2; }
+        else if (p.z >= lo2 && p.z < m2) { hi2 = m2; }
+        else ok = false;
+        if (!ok) break;
+        size = __fsub_rn(hi0, lo0);
+        key = (key << 3) | (uint64_t)oct;
+        ++d;
     }
-    const uint32_t in_b = __ballot_sync(0xffffffffu, inside);
-    const uint32_t gap_b = __ballot_sync(0xffffffffu, gap);
-    if ((threadIdx.x & 31) == 0) {
-        if (in_b) atomicAdd(&counters[TC_NIN], __popc(in_b));
-        if (gap_b) atomicAdd(&counters[TC_GAPS], __popc(gap_b));
+    if (d < D) {   // a gap between float child bounds: left-align the path
+        key <<= 3 * (D - d);
+        gap = true;
     }
+    return key;
 }
 
-// ------------------------------------------------------------ K3 radix sort --
-__global__ void __launch_bounds__(kSortThreads) k_sort_ghist(const uint64_t* __restrict__ keys,
-                                                             uint32_t* __restrict__ ghist) {
-    __shared__ uint32_t h[kPasses][256];
-    for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile + threadIdx.x;
-    for (int it = 0; it < kSortItems; ++it) {
-        const uint64_t k = keys[base + it * kSortThreads];
-#pragma unroll
-        for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255], 1u);
-    }
+// Zeroes this tile's look-back status words: every radix pass's, and the
+// positions scan's.
+__device__ __forceinline__ void zero_tile_status(unsigned long long* sort_status, int ntiles,
+                                                 unsigned long long* pos_status) {
+    for (int p = 0; p < kPasses; ++p)
+        sort_status[((size_t)p * ntiles + blockIdx.x) * 256 + threadIdx.x] = 0ull;
+    if (threadIdx.x == 0) pos_status[blockIdx.x] = 0ull;
+}
+
+// Adds a tile's digit histograms of every pass into ghist (bins that are
+// zero in this tile cost nothing).
+__device__ __forceinline__ void flush_hist(uint32_t (*h)[256], uint32_t* ghist) {
     __syncthreads();
     for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) {
         const uint32_t v = (&h[0][0])[i];
@@ -131,13 +118,55 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_ghist(const uint64_t* __r
     }
 }
 
+// K2 + the radix sort's global histograms: one block per tile of kSortTile
+// keys (key ~0 past n); counts bodies inside the root and paths cut by gaps.
+__global__ void __launch_bounds__(kSortThreads) k_keys_hist(const float4* __restrict__ pos, int n, float half, int D,
+                                                            uint64_t* __restrict__ keys, int32_t* __restrict__ vals,
+                                                            int32_t* __restrict__ depth,
+                                                            int32_t* __restrict__ counters, uint32_t* __restrict__ ghist,
+                                                            unsigned long long* __restrict__ sort_status, int ntiles,
+                                                            unsigned long long* __restrict__ pos_status) {
+    __shared__ uint32_t h[kPasses][256];
+    for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    zero_tile_status(sort_status, ntiles, pos_status);
+    __syncthreads();
+    for (int it = 0; it < kSortItems; ++it) {
+        const int i = blockIdx.x * kSortTile + it * kSortThreads + threadIdx.x;
+        vals[i] = i;
+        bool inside = false, gap = false;
+        uint64_t key = ~0ull;
+        if (i < n) {
+            int d;
+            key = body_key(pos[i], half, D, inside, gap, d);
+            depth[i] = d;
+        }
+        keys[i] = key;
+#pragma unroll
+        for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(key >> (8 * p)) & 255], 1u);
+        const uint32_t in_b = __ballot_sync(0xffffffffu, inside);
+        const uint32_t gap_b = __ballot_sync(0xffffffffu, gap);
+        if ((threadIdx.x & 31) == 0) {
+            if (in_b) atomicAdd(&counters[TC_NIN], __popc(in_b));
+            if (gap_b) atomicAdd(&counters[TC_GAPS], __popc(gap_b));
+        }
+    }
+    flush_hist(h, ghist);
+}
+
+// ------------------------------------------------------------ K3 radix sort --
 // plan[p] = 1 when every key has the same digit in pass p; plan[8+p] = buffer
-// the pass reads; plan[16] = buffer holding the result.
-__global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t* __restrict__ plan) {
+// the pass reads; plan[16] = buffer holding the result.  dig_off[p][d] = keys
+// with a smaller digit than d in pass p (where digit d's keys start).
+__global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t* __restrict__ plan,
+                            int32_t* __restrict__ dig_off) {
     __shared__ int triv[kPasses];
+    __shared__ int sh_warp[33];
     for (int p = 0; p < kPasses; ++p) {
-        const int t = __syncthreads_or(ghist[p * 256 + threadIdx.x] == (uint32_t)nk);
+        const int c = (int)ghist[p * 256 + threadIdx.x];
+        const int t = __syncthreads_or(c == nk);
         if (threadIdx.x == 0) triv[p] = t;
+        int total;
+        dig_off[p * 256 + threadIdx.x] = block_excl_scan(c, sh_warp, &total);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -151,25 +180,16 @@ __global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t*
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_hist(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+// One pass of the stable LSD sort in one launch (the one-sweep scheme,
+// Adinets and Merrill 2022): a tile ranks its keys by the pass's digit
+// (warp match_any, warps in order: stable), publishes its digit counts and
+// finds where earlier tiles put theirs by decoupled look-back, then scatters.
+__global__ void __launch_bounds__(kSortThreads) k_sort_pass(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+                                                            int32_t* __restrict__ v0, int32_t* __restrict__ v1,
                                                             int ntiles, const int32_t* __restrict__ plan, int pass,
-                                                            int32_t* __restrict__ hist) {
-    if (plan[pass]) return;
-    const uint64_t* keys = plan[8 + pass] ? k1 : k0;
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const int shift = 8 * pass;
-    const int base = blockIdx.x * kSortTile + threadIdx.x;
-    for (int it = 0; it < kSortItems; ++it) atomicAdd(&h[(keys[base + it * kSortThreads] >> shift) & 255], 1u);
-    __syncthreads();
-    hist[threadIdx.x * ntiles + blockIdx.x] = (int32_t)h[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
-                                                               int32_t* __restrict__ v0, int32_t* __restrict__ v1,
-                                                               int ntiles, const int32_t* __restrict__ hist,
-                                                               const int32_t* __restrict__ plan, int pass) {
+                                                            const int32_t* __restrict__ dig_off,
+                                                            unsigned long long* __restrict__ status,
+                                                            int* __restrict__ tile_ctr, int* __restrict__ err) {
     if (plan[pass]) return;
     const int src = plan[8 + pass];
     const uint64_t* ks = src ? k1 : k0;
@@ -178,11 +198,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(uint64_t* __restr
     int32_t* vd = src ? v0 : v1;
     __shared__ uint32_t whist[kSortWarps][256];
     __shared__ int32_t gbase[256];
+    __shared__ int sh_tile;
+    const int tile = lb_tile_index(tile_ctr, &sh_tile);
+    if (tile >= ntiles) return;   // cannot happen with one block per tile; kept as a guard
     for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int shift = 8 * pass;
-    const int base = blockIdx.x * kSortTile + warp * (32 * kSortItems) + lane;
+    const int base = tile * kSortTile + warp * (32 * kSortItems) + lane;
     uint64_t k[kSortItems];
     int32_t v[kSortItems];
     uint32_t r[kSortItems];
@@ -212,7 +235,16 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(uint64_t* __restr
             whist[w][d] = run;
             run += c;
         }
-        gbase[d] = hist[d * ntiles + blockIdx.x];
+        unsigned long long* st = status + (size_t)tile * 256 + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            lb_publish(st, 2u, run);
+        } else {
+            lb_publish(st, 1u, run);
+            excl = lb_exclusive(status + d, tile, 256, err);
+            lb_publish(st, 2u, excl + run);
+        }
+        gbase[d] = dig_off[pass * 256 + d] + (int)excl;
     }
     __syncthreads();
 #pragma unroll
@@ -310,59 +342,115 @@ __device__ void node_bounds(uint64_t code, int level, float half, float3& lo, fl
     side = size;
 }
 
-__global__ void k_gather(const float4* __restrict__ pos, const int32_t* __restrict__ vals, int n,
-                         float4* __restrict__ spos) {
+// Positions in sorted order; brings the sort result to buffer 0 when the
+// device plan left it in buffer 1 (no host read of the plan).
+__global__ void k_gather_final(const float4* __restrict__ pos, uint64_t* __restrict__ k0,
+                               const uint64_t* __restrict__ k1, int32_t* __restrict__ v0,
+                               const int32_t* __restrict__ v1, int n, const int32_t* __restrict__ plan,
+                               float4* __restrict__ spos) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < n) {
-        const int v = vals[s];
-        spos[s] = (v >= 0 && v < n) ? pos[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (s >= n) return;
+    const bool from1 = plan[16] != 0;
+    const int v = from1 ? v1[s] : v0[s];
+    if (from1) {
+        k0[s] = k1[s];
+        v0[s] = v;
     }
+    spos[s] = (v >= 0 && v < n) ? pos[v] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__global__ void k_positions(TopoView tv, const float4* __restrict__ spos, int32_t* __restrict__ pos_nint,
-                            int32_t* __restrict__ leaf_level, int32_t* __restrict__ leaf_count,
-                            int32_t* __restrict__ counters) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    bool leaf = false, deeper = false;
-    if (s < tv.n_total) {
-        tv.n_in = counters[TC_NIN];
-        int lo, hi, nint, lf, cur;
-        if (s < tv.n_in) {
-            tv.info(s, lo, hi, nint, lf, cur);
-        } else {
-            nint = 0; lf = -1; cur = -1;
-        }
-        int count = 0;
-        if (lf >= 0) {
-            count = 1;
-            if (lf == tv.D && cur == tv.D) {
-                int x = s;
-                const float4 p0 = spos[s];
-                while (x + 1 < tv.n_in && tv.delta(x) == tv.D) {
-                    ++x;
-                    ++count;
-                    const float4 q = spos[x];
-                    if (q.x != p0.x || q.y != p0.y || q.z != p0.z) deeper = true;
-                }
+// Internal nodes and leaf starting at sorted position s; bucket size and
+// whether a bucket's bodies differ.
+__device__ __forceinline__ void position_nodes(const TopoView& tv, const float4* spos, int s, int& nint, int& lf,
+                                               int& count, bool& deeper) {
+    int lo, hi, cur;
+    count = 0;
+    deeper = false;
+    if (s < tv.n_in) {
+        tv.info(s, lo, hi, nint, lf, cur);
+    } else {
+        nint = 0; lf = -1; cur = -1;
+    }
+    if (lf >= 0) {
+        count = 1;
+        if (lf == tv.D && cur == tv.D) {
+            int x = s;
+            const float4 p0 = spos[s];
+            while (x + 1 < tv.n_in && tv.delta(x) == tv.D) {
+                ++x;
+                ++count;
+                const float4 q = spos[x];
+                if (q.x != p0.x || q.y != p0.y || q.z != p0.z) deeper = true;
             }
-            leaf = true;
         }
-        pos_nint[s] = nint;
-        leaf_level[s] = lf;
-        leaf_count[s] = count;
-    }
-    const uint32_t lb = __ballot_sync(0xffffffffu, leaf);
-    const uint32_t db = __ballot_sync(0xffffffffu, deeper);
-    if ((threadIdx.x & 31) == 0) {
-        if (lb) atomicAdd(&counters[TC_NLEAF], __popc(lb));
-        if (db) atomicAdd(&counters[TC_DEEPER], __popc(db));
     }
 }
 
+// Per tile of kSortTile sorted positions (kSortItems consecutive ones per
+// thread): the nodes starting there, and the exclusive prefix of their
+// internal-node counts by single-pass scan (pos_nint; the total goes to
+// counters[TC_NINT]).  With hk_zero, the threads also clear the internal-node
+// hash table for the emission that follows.
+__global__ void __launch_bounds__(kSortThreads) k_positions_scan(TopoView tv, const float4* __restrict__ spos,
+                                                                 int32_t* __restrict__ pos_nint,
+                                                                 int32_t* __restrict__ leaf_level,
+                                                                 int32_t* __restrict__ leaf_count,
+                                                                 int32_t* __restrict__ counters,
+                                                                 unsigned long long* __restrict__ status, int ntiles,
+                                                                 uint64_t* __restrict__ hk_zero, int hk_n,
+                                                                 int* __restrict__ err) {
+    __shared__ int sh_warp[33], sh_off, sh_tile;
+    if (hk_zero)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < hk_n; i += gridDim.x * blockDim.x) hk_zero[i] = 0ull;
+    const int tile = lb_tile_index(&counters[TC_TILE_POS], &sh_tile);
+    tv.n_in = counters[TC_NIN];
+    const int s0 = tile * kSortTile + threadIdx.x * kSortItems;
+    int nint[kSortItems];
+    int sum = 0;
+    unsigned nleaf = 0, ndeeper = 0;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int s = s0 + k;
+        nint[k] = 0;
+        if (s < tv.n_total) {
+            int lf, count;
+            bool deeper;
+            position_nodes(tv, spos, s, nint[k], lf, count, deeper);
+            leaf_level[s] = lf;
+            leaf_count[s] = count;
+            nleaf += lf >= 0 ? 1u : 0u;
+            ndeeper += deeper ? 1u : 0u;
+        }
+        sum += nint[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nleaf += __shfl_xor_sync(0xffffffffu, nleaf, o);
+        ndeeper += __shfl_xor_sync(0xffffffffu, ndeeper, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (nleaf) atomicAdd(&counters[TC_NLEAF], (int)nleaf);
+        if (ndeeper) atomicAdd(&counters[TC_DEEPER], (int)ndeeper);
+    }
+    int run = lb_scan_tile(sum, tile, ntiles, status, counters + TC_NINT, sh_warp, &sh_off, err);
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int s = s0 + k;
+        if (s < tv.n_total) pos_nint[s] = run;
+        run += nint[k];
+    }
+}
+
+// Emits the internal nodes starting at each sorted position (level, first
+// body, code, hash entry) and clears their child mask and counters, and the
+// look-back status of the child-count scan.
 __global__ void k_emit(TopoView tv, const int32_t* __restrict__ int_base, int32_t* __restrict__ int_level,
                        int32_t* __restrict__ int_first, uint64_t* __restrict__ int_code, uint64_t* __restrict__ hk,
-                       int32_t* __restrict__ hv, uint32_t hmask, int32_t* __restrict__ counters) {
+                       int32_t* __restrict__ hv, uint32_t hmask, uint32_t* __restrict__ int_mask,
+                       int32_t* __restrict__ int_nint, int32_t* __restrict__ int_pending,
+                       int32_t* __restrict__ counters, unsigned long long* __restrict__ popc_status,
+                       int popc_tiles) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = s; i < popc_tiles; i += gridDim.x * blockDim.x) popc_status[i] = 0ull;   // for k_popc_scan
     if (s >= tv.n_in) return;
     int lo, hi, nint, lf, cur;
     tv.info(s, lo, hi, nint, lf, cur);
@@ -378,18 +466,20 @@ __global__ void k_emit(TopoView tv, const int32_t* __restrict__ int_base, int32_
         int_level[k] = l;
         int_first[k] = s;
         int_code[k] = code;
+        int_mask[k] = 0u;
+        int_nint[k] = 0;
+        int_pending[k] = 0;
         hash_insert(hk, hv, hmask, code, k, counters);
     }
 }
 
-__global__ void k_link_internal(const int32_t* __restrict__ int_level, const int32_t* __restrict__ int_first,
-                                const uint64_t* __restrict__ int_code, TopoView tv, int n_int,
-                                const int32_t* __restrict__ n_int_dev,
-                                const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv, uint32_t hmask,
-                                int32_t* __restrict__ int_parent, uint32_t* __restrict__ int_mask,
-                                int32_t* __restrict__ int_nint, int32_t* __restrict__ counters) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+__device__ __forceinline__ void link_internal(int k, const int32_t* __restrict__ int_level,
+                                              const int32_t* __restrict__ int_first,
+                                              const uint64_t* __restrict__ int_code, const TopoView& tv, int ni,
+                                              const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv,
+                                              uint32_t hmask, int32_t* __restrict__ int_parent,
+                                              uint32_t* __restrict__ int_mask, int32_t* __restrict__ int_nint,
+                                              int32_t* __restrict__ counters) {
     if (k >= ni || k == 0) return;
     const int l = int_level[k];
     const int s = int_first[k];
@@ -405,11 +495,11 @@ __global__ void k_link_internal(const int32_t* __restrict__ int_level, const int
     atomicAdd(&int_nint[parent], 1);
 }
 
-__global__ void k_link_leaves(TopoView tv, const int32_t* __restrict__ int_base, const int32_t* __restrict__ leaf_level,
-                              const uint64_t* __restrict__ hk, const int32_t* __restrict__ hv, uint32_t hmask,
-                              int32_t* __restrict__ leaf_parent, uint32_t* __restrict__ int_mask,
-                              int32_t* __restrict__ counters) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void link_leaf(int s, const TopoView& tv, const int32_t* __restrict__ int_base,
+                                          const int32_t* __restrict__ leaf_level, const uint64_t* __restrict__ hk,
+                                          const int32_t* __restrict__ hv, uint32_t hmask,
+                                          int32_t* __restrict__ leaf_parent, uint32_t* __restrict__ int_mask,
+                                          int32_t* __restrict__ counters) {
     if (s >= tv.n_in) return;
     const int lf = leaf_level[s];
     if (lf <= 0) return;
@@ -425,11 +515,49 @@ __global__ void k_link_leaves(TopoView tv, const int32_t* __restrict__ int_base,
     atomicOr(&int_mask[parent], 1u << (unsigned)(code & 7ull));
 }
 
-__global__ void k_popc(const uint32_t* __restrict__ mask, int n_int, const int32_t* __restrict__ n_int_dev,
-                       int32_t* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+// Every node's parent and the parents' child masks: blocks [0, int_blocks)
+// link internal nodes, the rest link the leaf starting at each position.
+// n_int_dev (graph builds) bounds the internal nodes by the device count.
+__global__ void k_link(const int32_t* __restrict__ int_level, const int32_t* __restrict__ int_first,
+                       const uint64_t* __restrict__ int_code, TopoView tv, int n_int,
+                       const int32_t* __restrict__ n_int_dev, int int_blocks, const int32_t* __restrict__ int_base,
+                       const int32_t* __restrict__ leaf_level, const uint64_t* __restrict__ hk,
+                       const int32_t* __restrict__ hv, uint32_t hmask, int32_t* __restrict__ int_parent,
+                       int32_t* __restrict__ leaf_parent, uint32_t* __restrict__ int_mask,
+                       int32_t* __restrict__ int_nint, int32_t* __restrict__ counters) {
+    if ((int)blockIdx.x < int_blocks) {
+        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+        const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+        link_internal(k, int_level, int_first, int_code, tv, ni, hk, hv, hmask, int_parent, int_mask, int_nint,
+                      counters);
+    } else {
+        const int s = (blockIdx.x - int_blocks) * blockDim.x + threadIdx.x;
+        link_leaf(s, tv, int_base, leaf_level, hk, hv, hmask, leaf_parent, int_mask, counters);
+    }
+}
+
+// int_block[k] = non-empty children of internal nodes before k (their first
+// child cell, less one), by single-pass scan over tiles of kSortTile nodes.
+__global__ void __launch_bounds__(kSortThreads) k_popc_scan(const uint32_t* __restrict__ mask, int n_int,
+                                                            const int32_t* __restrict__ n_int_dev,
+                                                            int32_t* __restrict__ out, int32_t* __restrict__ counters,
+                                                            unsigned long long* __restrict__ status, int ntiles,
+                                                            int* __restrict__ err) {
+    __shared__ int sh_warp[33], sh_off, sh_tile;
+    const int tile = lb_tile_index(&counters[TC_TILE_POPC], &sh_tile);
     const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
-    if (k < n_int) out[k] = k < ni ? __popc(mask[k]) : 0;
+    const int k0 = tile * kSortTile + threadIdx.x * kSortItems;
+    int c[kSortItems];
+    int sum = 0;
+    for (int k = 0; k < kSortItems; ++k) {
+        c[k] = (k0 + k < ni) ? __popc(mask[k0 + k]) : 0;
+        sum += c[k];
+    }
+    int run = lb_scan_tile(sum, tile, ntiles, status, nullptr, sh_warp, &sh_off, err);
+    for (int k = 0; k < kSortItems; ++k) {
+        if (k0 + k < n_int) out[k0 + k] = run;
+        run += c[k];
+    }
 }
 
 // Opening thresholds of a cell for the traversal: with r^2 computed exactly
@@ -447,15 +575,14 @@ __device__ __forceinline__ int child_cell(const int32_t* int_block, const uint32
     return 1 + int_block[parent] + __popc(int_mask[parent] & ((1u << oct) - 1u));
 }
 
-__global__ void k_place_internal(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
-                                 const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
-                                 const int32_t* __restrict__ int_block, int n_int,
-                                 const int32_t* __restrict__ n_int_dev, int cell_cap, float half, float theta_f,
-                                 int32_t* __restrict__ int_cell, int4* __restrict__ cell_meta,
-                                 float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
-                                 uint64_t* __restrict__ cell_code) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+__device__ __forceinline__ void place_internal(int k, const int32_t* __restrict__ int_level,
+                                               const uint64_t* __restrict__ int_code,
+                                               const int32_t* __restrict__ int_parent,
+                                               const uint32_t* __restrict__ int_mask,
+                                               const int32_t* __restrict__ int_block, int ni, int cell_cap,
+                                               float half, float theta_f, int32_t* __restrict__ int_cell,
+                                               int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
+                                               float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
     if (k >= ni) return;
     const uint64_t code = int_code[k];
     const int l = int_level[k];
@@ -477,15 +604,15 @@ __global__ void k_place_internal(const int32_t* __restrict__ int_level, const ui
     cell_code[cell] = code;
 }
 
-__global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_level,
-                               const int32_t* __restrict__ leaf_count, const int32_t* __restrict__ leaf_parent,
-                               const uint32_t* __restrict__ int_mask, const int32_t* __restrict__ int_block,
-                               const float4* __restrict__ spos, float half, float theta_f,
-                               float4* __restrict__ cell_com, double* __restrict__ cell_mass,
-                               int32_t* __restrict__ cell_count, int4* __restrict__ cell_meta,
-                               float4* __restrict__ cell_lo, float4* __restrict__ cell_hi,
-                               uint64_t* __restrict__ cell_code) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void place_leaf(int s, const TopoView& tv, const int32_t* __restrict__ leaf_level,
+                                           const int32_t* __restrict__ leaf_count,
+                                           const int32_t* __restrict__ leaf_parent,
+                                           const uint32_t* __restrict__ int_mask,
+                                           const int32_t* __restrict__ int_block, const float4* __restrict__ spos,
+                                           float half, float theta_f, float4* __restrict__ cell_com,
+                                           double* __restrict__ cell_mass, int32_t* __restrict__ cell_count,
+                                           int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
+                                           float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
     if (s >= tv.n_in) return;
     const int lf = leaf_level[s];
     if (lf < 0) return;
@@ -531,6 +658,30 @@ __global__ void k_place_leaves(TopoView tv, const int32_t* __restrict__ leaf_lev
     cell_lo[cell] = make_float4(lo.x, lo.y, lo.z, side);
     cell_hi[cell] = make_float4(hi.x, hi.y, hi.z, (float)lf);
     cell_code[cell] = code;
+}
+
+// Every cell: blocks [0, int_blocks) place internal nodes (bounds, opening
+// thresholds, first child), the rest the leaf starting at each position
+// (bounds, thresholds, mass and centre of mass of its body or bucket).
+__global__ void k_place(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
+                        const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
+                        const int32_t* __restrict__ int_block, int n_int, const int32_t* __restrict__ n_int_dev,
+                        int int_blocks, TopoView tv, const int32_t* __restrict__ leaf_level,
+                        const int32_t* __restrict__ leaf_count, const int32_t* __restrict__ leaf_parent,
+                        const float4* __restrict__ spos, float half, float theta_f, int32_t* __restrict__ int_cell,
+                        float4* __restrict__ cell_com, double* __restrict__ cell_mass,
+                        int32_t* __restrict__ cell_count, int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
+                        float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
+    if ((int)blockIdx.x < int_blocks) {
+        const int k = blockIdx.x * blockDim.x + threadIdx.x;
+        const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
+        place_internal(k, int_level, int_code, int_parent, int_mask, int_block, ni, tv.cell_cap, half, theta_f,
+                       int_cell, cell_meta, cell_lo, cell_hi, cell_code);
+    } else {
+        const int s = (blockIdx.x - int_blocks) * blockDim.x + threadIdx.x;
+        place_leaf(s, tv, leaf_level, leaf_count, leaf_parent, int_mask, int_block, spos, half, theta_f, cell_com,
+                   cell_mass, cell_count, cell_meta, cell_lo, cell_hi, cell_code);
+    }
 }
 
 // ------------------------------------------------------------- K5 mass ----
@@ -584,6 +735,39 @@ __global__ void k_mass(int n_int, const int32_t* __restrict__ n_int_dev, const i
     }
 }
 
+// ------------------------------------------------- batched forest keys ----
+// Keys of the batched form's Barnes-Hut bodies [0, n) (nb_morton.cuh), with
+// the radix sort's histograms and the look-back status cleared, one block per
+// sort tile; the first threads also write each galaxy's cube for the
+// traversal.  Pad entries [n, tiles * kSortTile) get key ~0.
+__global__ void __launch_bounds__(kSortThreads) k_batch_keys_hist(
+    const float4* __restrict__ pos, const int32_t* __restrict__ body_slot, int n, const unsigned* __restrict__ box_bits,
+    int nslot, float4* __restrict__ gal_box, uint64_t* __restrict__ keys, int32_t* __restrict__ vals,
+    int32_t* __restrict__ depth, uint32_t* __restrict__ ghist, unsigned long long* __restrict__ sort_status,
+    int ntiles, unsigned long long* __restrict__ pos_status) {
+    __shared__ uint32_t h[kPasses][256];
+    const int g = blockIdx.x * kSortThreads + threadIdx.x;
+    if (g < nslot) gal_box[g] = gal_cube(box_bits, g);
+    if ((int)blockIdx.x >= ntiles) return;   // blocks past the keys only write galaxy cubes (block-uniform)
+    for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    zero_tile_status(sort_status, ntiles, pos_status);
+    __syncthreads();
+    for (int it = 0; it < kSortItems; ++it) {
+        const int i = blockIdx.x * kSortTile + it * kSortThreads + threadIdx.x;
+        vals[i] = i;
+        uint64_t key = ~0ull;
+        if (i < n) {
+            const int slot = body_slot[i];
+            key = forest_key(pos[i], slot, gal_cube(box_bits, slot));
+            depth[i] = kBatchDepth;
+        }
+        keys[i] = key;
+#pragma unroll
+        for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(key >> (8 * p)) & 255], 1u);
+    }
+    flush_hist(h, ghist);
+}
+
 // --------------------------------------------------------------- host ----
 static cudaError_t grow(void** p, size_t bytes) {
     if (*p) cudaFree(*p);
@@ -612,23 +796,18 @@ static cudaError_t reserve_bodies(nb_sim* sim, size_t nk) {
     NB_TRY(grow((void**)&t.leaf_count, cap * 4));
     NB_TRY(grow((void**)&t.leaf_parent, cap * 4));
     const size_t ntiles = cap / kSortTile;
-    t.hist_cap = 256 * ntiles;
-    NB_TRY(grow((void**)&t.hist, t.hist_cap * 4));
-    if (!t.ghist) NB_TRY(cudaMalloc(&t.ghist, kPasses * 256 * 4));
+    NB_TRY(grow((void**)&t.sort_status, (size_t)kPasses * ntiles * 256 * sizeof(unsigned long long)));
+    NB_TRY(grow((void**)&t.pos_status, ntiles * sizeof(unsigned long long)));
     if (!t.plan) NB_TRY(cudaMalloc(&t.plan, 32 * 4));
-    if (!t.counters) NB_TRY(cudaMalloc(&t.counters, TC_COUNT * 4));
+    if (!t.dig_off) NB_TRY(cudaMalloc(&t.dig_off, kPasses * 256 * 4));
+    if (!t.counters) {
+        // counters, tile counters of the look-back kernels, then the radix histograms
+        NB_TRY(cudaMalloc(&t.counters, (kCounterWords + kPasses * 256) * 4));
+        t.ghist = reinterpret_cast<uint32_t*>(t.counters + kCounterWords);
+    }
     if (!t.h_counters) NB_TRY(cudaMallocHost(&t.h_counters, TC_COUNT * 4));
     if (!t.interactions) NB_TRY(cudaMalloc(&t.interactions, sizeof(unsigned long long)));
     t.body_cap = cap;
-    return cudaSuccess;
-}
-
-static cudaError_t reserve_scan(nb_sim* sim, size_t n) {
-    TreeBuffers& t = sim->tree;
-    const size_t need = (size_t)scan_blocks((int)n) + 1;
-    if (need <= t.scan_cap) return cudaSuccess;
-    NB_TRY(grow((void**)&t.scan_sums, need * 4));
-    t.scan_cap = need;
     return cudaSuccess;
 }
 
@@ -645,6 +824,9 @@ static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
         NB_TRY(grow((void**)&t.int_block, cap * 4));
         NB_TRY(grow((void**)&t.int_cell, cap * 4));
         NB_TRY(grow((void**)&t.int_code, cap * 8));
+        // internal nodes can outnumber bodies (chains of one-child nodes above
+        // close pairs): the child-count scan's status is sized by them
+        NB_TRY(grow((void**)&t.popc_status, ((cap + kSortTile - 1) / kSortTile) * sizeof(unsigned long long)));
         t.int_cap = cap;
         size_t h = 1024;
         while (h < 2 * cap) h <<= 1;
@@ -663,14 +845,11 @@ static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
         NB_TRY(grow((void**)&t.cell_code, cap * 8));
         t.cell_cap = cap;
     }
-    // the batched build scans the whole internal-node capacity
-    return reserve_scan(sim, std::max(t.int_cap, (size_t)1));
+    return cudaSuccess;
 }
 
 cudaError_t tree_reserve(nb_sim* sim) {
-    const size_t nk = pad_up(std::max<size_t>(sim->n, 1), kSortTile);
-    NB_TRY(reserve_bodies(sim, nk));
-    return reserve_scan(sim, std::max(nk, (size_t)256 * (nk / kSortTile)));
+    return reserve_bodies(sim, pad_up(std::max<size_t>(sim->n, 1), kSortTile));
 }
 
 void tree_free(nb_sim* sim) {
@@ -678,8 +857,8 @@ void tree_free(nb_sim* sim) {
     void* ptrs[] = {t.keys[0], t.keys[1], t.vals[0], t.vals[1], t.depth, t.spos, t.pos_nint, t.leaf_level,
                     t.leaf_count, t.leaf_parent, t.int_level, t.int_first, t.int_parent, t.int_mask, t.int_nint,
                     t.int_pending, t.int_block, t.int_cell, t.int_code, t.cell_com, t.cell_meta, t.cell_mass,
-                    t.cell_lo, t.cell_hi, t.cell_code, t.cell_count, t.hkeys, t.hvals, t.hist, t.ghist, t.plan, t.scan_sums,
-                    t.counters, t.interactions};
+                    t.cell_lo, t.cell_hi, t.cell_code, t.cell_count, t.hkeys, t.hvals, t.sort_status, t.pos_status,
+                    t.popc_status, t.dig_off, t.plan, t.counters, t.interactions};
     for (void* p : ptrs) cudaFree(p);
     if (t.h_counters) cudaFreeHost(t.h_counters);
     t = TreeBuffers{};
@@ -705,18 +884,33 @@ static TopoView topo_view(nb_sim* sim) {
     return tv;
 }
 
-// Keys of the current positions into t.keys[0] (input order), t.vals[0] = identity.
+// Clears the counters and histograms, then keys of the current positions into
+// t.keys[0] (input order, t.vals[0] = identity) with their histograms.
 static cudaError_t launch_keys(nb_sim* sim, size_t nk) {
     TreeBuffers& t = sim->tree;
+    const int ntiles = (int)(nk / kSortTile);
+    NB_TRY(cudaMemsetAsync(t.counters, 0, (kCounterWords + kPasses * 256) * 4, sim->stream));
     PhaseScope ps(sim, NB_PHASE_KEYS);
-    k_keys<<<(unsigned)((nk + 255) / 256), 256, 0, sim->stream>>>(sim->pos, (int)sim->n, (int)nk,
-                                                                 sim->prm.bounds_half, sim->prm.max_depth,
-                                                                 t.keys[0], t.vals[0], t.depth, t.counters);
+    k_keys_hist<<<ntiles, kSortThreads, 0, sim->stream>>>(sim->pos, (int)sim->n, sim->prm.bounds_half,
+                                                          sim->prm.max_depth, t.keys[0], t.vals[0], t.depth,
+                                                          t.counters, t.ghist, t.sort_status, ntiles, t.pos_status);
     return cudaGetLastError();
 }
 
-__global__ void k_sort_finalize(uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1, int32_t* __restrict__ v0,
-                                const int32_t* __restrict__ v1, int n, const int32_t* __restrict__ plan);
+// The radix sort of t.keys[0] / t.vals[0] (histograms already made): the
+// device plan, then one launch per pass.
+static cudaError_t launch_sort(nb_sim* sim, size_t nk) {
+    TreeBuffers& t = sim->tree;
+    const int ntiles = (int)(nk / kSortTile);
+    cudaStream_t st = sim->stream;
+    PhaseScope ps(sim, NB_PHASE_SORT, 1 + kPasses);
+    k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan, t.dig_off);
+    for (int p = 0; p < kPasses; ++p)
+        k_sort_pass<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles, t.plan, p,
+                                                     t.dig_off, t.sort_status + (size_t)p * ntiles * 256,
+                                                     t.counters + TC_TILE_SORT + p, sim->d_err);
+    return cudaGetLastError();
+}
 
 cudaError_t tree_build(nb_sim* sim) {
     TreeBuffers& t = sim->tree;
@@ -725,33 +919,20 @@ cudaError_t tree_build(nb_sim* sim) {
     const int ntiles = (int)(nk / kSortTile);
     NB_TRY(tree_reserve(sim));
     cudaStream_t st = sim->stream;
-    NB_TRY(cudaMemsetAsync(t.counters, 0, TC_COUNT * 4, st));
     NB_TRY(launch_keys(sim, nk));
-    {
-        PhaseScope ps(sim, NB_PHASE_SORT, 2 + kPasses * 5);
-        NB_TRY(cudaMemsetAsync(t.ghist, 0, kPasses * 256 * 4, st));
-        k_sort_ghist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.ghist);
-        k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan);
-        for (int p = 0; p < kPasses; ++p) {
-            k_sort_hist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], ntiles, t.plan, p, t.hist);
-            NB_TRY(exclusive_scan(t.hist, t.hist, 256 * ntiles, t.scan_sums, nullptr, st, t.plan + p));
-            k_sort_scatter<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles,
-                                                            t.hist, t.plan, p);
-        }
-        NB_TRY(cudaGetLastError());
-    }
+    NB_TRY(launch_sort(sim, nk));
     // The sort result's buffer is decided on the device (passes with a constant
-    // digit are skipped): a copy on the device brings it to buffer 0 when it
-    // ended in buffer 1, so no host read is needed here.
+    // digit are skipped): the gather brings it to buffer 0 when it ended in
+    // buffer 1, so no host read is needed here.
     {
-        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 4);
-        k_sort_finalize<<<(n + 255) / 256, 256, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], n, t.plan);
+        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 2);
+        k_gather_final<<<(n + 255) / 256, 256, 0, st>>>(sim->pos, t.keys[0], t.keys[1], t.vals[0], t.vals[1], n,
+                                                        t.plan, t.spos);
         t.final_buf = 0;
-        k_gather<<<(n + 255) / 256, 256, 0, st>>>(sim->pos, t.vals[0], n, t.spos);
         TopoView tv = topo_view(sim);
-        k_positions<<<(n + 255) / 256, 256, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters);
-        NB_TRY(exclusive_scan(t.pos_nint, t.pos_nint, n, t.scan_sums, t.counters + TC_NINT, st));
-        NB_TRY(cudaMemcpyAsync(t.h_counters, t.counters, TC_COUNT * 4 - 4, cudaMemcpyDeviceToHost, st));
+        k_positions_scan<<<ntiles, kSortThreads, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count,
+                                                          t.counters, t.pos_status, ntiles, nullptr, 0, sim->d_err);
+        NB_TRY(cudaMemcpyAsync(t.h_counters, t.counters, TC_COUNT * 4, cudaMemcpyDeviceToHost, st));
         NB_TRY(cudaStreamSynchronize(st));
     }
     t.n_in = t.h_counters[TC_NIN];
@@ -765,29 +946,23 @@ cudaError_t tree_build(nb_sim* sim) {
     const float tf = theta_float(sim->prm.theta);
     const uint32_t hmask = (uint32_t)(t.hash_cap - 1);
     {
-        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 6);
+        PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 4);
         NB_TRY(cudaMemsetAsync(t.hkeys, 0, t.hash_cap * 8, st));
-        NB_TRY(cudaMemsetAsync(t.int_mask, 0, (size_t)ni * 4, st));
-        NB_TRY(cudaMemsetAsync(t.int_nint, 0, (size_t)ni * 4, st));
-        NB_TRY(cudaMemsetAsync(t.int_pending, 0, (size_t)ni * 4, st));
         const int nbk = (t.n_in + kEmitBlock - 1) / kEmitBlock;
+        const int ib = (ni + kEmitBlock - 1) / kEmitBlock;
+        const int ptiles = (ni + kSortTile - 1) / kSortTile;
         k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals,
-                                          hmask, t.counters);
-        k_link_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, ni, nullptr, t.hkeys,
-                                                         t.hvals, hmask, t.int_parent, t.int_mask, t.int_nint,
-                                                         t.counters);
-        k_link_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask,
-                                                 t.leaf_parent, t.int_mask, t.counters);
-        k_popc<<<(ni + 255) / 256, 256, 0, st>>>(t.int_mask, ni, nullptr, t.int_block);
-        NB_TRY(exclusive_scan(t.int_block, t.int_block, ni, t.scan_sums, nullptr, st));
-        k_place_internal<<<(ni + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
-                                                          t.int_block, ni, nullptr, (int)t.cell_cap, sim->prm.bounds_half,
-                                                          tf, t.int_cell,
-                                                          t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
-        k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask,
-                                                  t.int_block, t.spos, sim->prm.bounds_half, tf, t.cell_com,
-                                                  t.cell_mass, t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi,
-                                                  t.cell_code);
+                                          hmask, t.int_mask, t.int_nint, t.int_pending, t.counters, t.popc_status,
+                                          ptiles);
+        k_link<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, ni, nullptr, ib, t.pos_nint,
+                                               t.leaf_level, t.hkeys, t.hvals, hmask, t.int_parent, t.leaf_parent,
+                                               t.int_mask, t.int_nint, t.counters);
+        k_popc_scan<<<ptiles, kSortThreads, 0, st>>>(t.int_mask, ni, nullptr, t.int_block, t.counters,
+                                                     t.popc_status, ptiles, sim->d_err);
+        k_place<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask, t.int_block, ni,
+                                                nullptr, ib, tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.spos,
+                                                sim->prm.bounds_half, tf, t.int_cell, t.cell_com, t.cell_mass,
+                                                t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
         NB_TRY(cudaGetLastError());
     }
     {
@@ -812,7 +987,6 @@ cudaError_t tree_keys_export(nb_sim* sim, uint64_t* d_keys, int32_t* d_depth) {
     TreeBuffers& t = sim->tree;
     const size_t nk = pad_up(std::max<size_t>(sim->n, 1), kSortTile);
     NB_TRY(tree_reserve(sim));
-    NB_TRY(cudaMemsetAsync(t.counters, 0, TC_COUNT * 4, sim->stream));
     NB_TRY(launch_keys(sim, nk));
     NB_TRY(cudaMemcpyAsync(d_keys, t.keys[0], sim->n * 8, cudaMemcpyDeviceToDevice, sim->stream));
     NB_TRY(cudaMemcpyAsync(d_depth, t.depth, sim->n * 4, cudaMemcpyDeviceToDevice, sim->stream));
@@ -824,27 +998,27 @@ cudaError_t tree_keys_export(nb_sim* sim, uint64_t* d_keys, int32_t* d_depth) {
 
 // ----------------------------------------------------------------------------
 // Topology without host synchronisation, for the batched form (its steps are
-// captured in a CUDA graph).  The caller has written keys, depths and the
-// identity order of bodies [0, n) into keys[0] / depth / vals[0] (pad entries
-// up to the sort tile with key ~0) and reserved capacities; every body lies
-// inside its cube.  Grid sizes come from the capacities; the kernels read the
-// node counts on the device and report overflow in counters[TC_OVERFLOW].
+// captured in a CUDA graph).  The batched step's first kernel clears the
+// counters and histograms and sets TC_NIN = n; tree_batch_keys writes the
+// keys of bodies [0, n), their histograms and clears the look-back status
+// (every body lies inside its cube).  Grid sizes come from the capacities;
+// the kernels read the node counts on the device and report overflow in
+// counters[TC_OVERFLOW].
 // ----------------------------------------------------------------------------
 namespace nb {
 
-__global__ void k_counters_init(int32_t* __restrict__ counters, int n_in) {
-    if (threadIdx.x < TC_COUNT) counters[threadIdx.x] = threadIdx.x == TC_NIN ? n_in : 0;
-}
+int tree_counter_words() { return kCounterWords + kPasses * 256; }
 
-// Moves the sort result into buffer 0 when the device plan left it in buffer 1.
-__global__ void k_sort_finalize(uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1, int32_t* __restrict__ v0,
-                                const int32_t* __restrict__ v1, int n, const int32_t* __restrict__ plan) {
-    if (plan[16] == 0) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        k0[i] = k1[i];
-        v0[i] = v1[i];
-    }
+cudaError_t tree_batch_keys(nb_sim* sim, const float4* pos, const int32_t* body_slot, int n,
+                            const unsigned* box_bits, int nslot, float4* gal_box) {
+    TreeBuffers& t = sim->tree;
+    const int ntiles = (int)(pad_up(std::max<size_t>((size_t)n, 1), kSortTile) / kSortTile);
+    const int blocks = std::max(ntiles, (nslot + kSortThreads - 1) / kSortThreads);
+    PhaseScope ps(sim, NB_PHASE_KEYS);
+    k_batch_keys_hist<<<blocks, kSortThreads, 0, sim->stream>>>(pos, body_slot, n, box_bits, nslot, gal_box,
+                                                                t.keys[0], t.vals[0], t.depth, t.ghist,
+                                                                t.sort_status, ntiles, t.pos_status);
+    return cudaGetLastError();
 }
 
 cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
@@ -852,20 +1026,7 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
     const size_t nk = pad_up(std::max<size_t>((size_t)n, 1), kSortTile);
     const int ntiles = (int)(nk / kSortTile);
     cudaStream_t st = sim->stream;
-    {
-        PhaseScope ps(sim, NB_PHASE_SORT, 3 + kPasses * 5);
-        NB_TRY(cudaMemsetAsync(t.ghist, 0, kPasses * 256 * 4, st));
-        k_sort_ghist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.ghist);
-        k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan);
-        for (int p = 0; p < kPasses; ++p) {
-            k_sort_hist<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], ntiles, t.plan, p, t.hist);
-            NB_TRY(exclusive_scan(t.hist, t.hist, 256 * ntiles, t.scan_sums, nullptr, st, t.plan + p));
-            k_sort_scatter<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles,
-                                                            t.hist, t.plan, p);
-        }
-        k_sort_finalize<<<(n + 255) / 256, 256, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], n, t.plan);
-        NB_TRY(cudaGetLastError());
-    }
+    NB_TRY(launch_sort(sim, nk));
     t.final_buf = 0;
     t.n_in = n;
     TopoView tv;
@@ -880,39 +1041,33 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
     const int icap = (int)t.int_cap;
     const uint32_t hmask = (uint32_t)(t.hash_cap - 1);
     const int nbk = (n + kEmitBlock - 1) / kEmitBlock;
-    PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 12);
-    k_counters_init<<<1, 32, 0, st>>>(t.counters, n);
-    k_gather<<<(n + 255) / 256, 256, 0, st>>>(pos, t.vals[0], n, t.spos);
-    k_positions<<<(n + 255) / 256, 256, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters);
-    NB_TRY(exclusive_scan(t.pos_nint, t.pos_nint, n, t.scan_sums, t.counters + TC_NINT, st));
-    NB_TRY(cudaMemsetAsync(t.hkeys, 0, t.hash_cap * 8, st));
-    NB_TRY(cudaMemsetAsync(t.int_mask, 0, (size_t)icap * 4, st));
-    NB_TRY(cudaMemsetAsync(t.int_nint, 0, (size_t)icap * 4, st));
-    NB_TRY(cudaMemsetAsync(t.int_pending, 0, (size_t)icap * 4, st));
+    const int ib = (icap + kEmitBlock - 1) / kEmitBlock;
+    const int ptiles = (icap + kSortTile - 1) / kSortTile;
+    PhaseScope ps(sim, NB_PHASE_TOPOLOGY, 6);
+    k_gather_final<<<(n + 255) / 256, 256, 0, st>>>(pos, t.keys[0], t.keys[1], t.vals[0], t.vals[1], n, t.plan,
+                                                    t.spos);
+    // this scan also clears the internal-node hash table for the emission
+    k_positions_scan<<<ntiles, kSortThreads, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters,
+                                                      t.pos_status, ntiles, t.hkeys, (int)t.hash_cap, sim->d_err);
     k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals, hmask,
-                                      t.counters);
-    k_link_internal<<<(icap + 255) / 256, 256, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, icap,
-                                                       t.counters + TC_NINT, t.hkeys, t.hvals, hmask, t.int_parent,
-                                                       t.int_mask, t.int_nint, t.counters);
-    k_link_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask, t.leaf_parent,
-                                             t.int_mask, t.counters);
-    k_popc<<<(icap + 255) / 256, 256, 0, st>>>(t.int_mask, icap, t.counters + TC_NINT, t.int_block);
-    NB_TRY(exclusive_scan(t.int_block, t.int_block, icap, t.scan_sums, nullptr, st));
-    k_place_internal<<<(icap + 255) / 256, 256, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask,
-                                                        t.int_block, icap, t.counters + TC_NINT, (int)t.cell_cap,
-                                                        sim->prm.bounds_half, 1.0f, t.int_cell, t.cell_meta, t.cell_lo,
-                                                        t.cell_hi, t.cell_code);
-    k_place_leaves<<<nbk, kEmitBlock, 0, st>>>(tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.int_mask, t.int_block,
-                                              t.spos, sim->prm.bounds_half, 1.0f, t.cell_com, t.cell_mass,
-                                              t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+                                      t.int_mask, t.int_nint, t.int_pending, t.counters, t.popc_status, ptiles);
+    k_link<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, icap, t.counters + TC_NINT, ib,
+                                           t.pos_nint, t.leaf_level, t.hkeys, t.hvals, hmask, t.int_parent,
+                                           t.leaf_parent, t.int_mask, t.int_nint, t.counters);
+    k_popc_scan<<<ptiles, kSortThreads, 0, st>>>(t.int_mask, icap, t.counters + TC_NINT, t.int_block, t.counters,
+                                                 t.popc_status, ptiles, sim->d_err);
+    k_place<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask, t.int_block, icap,
+                                            t.counters + TC_NINT, ib, tv, t.leaf_level, t.leaf_count, t.leaf_parent,
+                                            t.spos, sim->prm.bounds_half, 1.0f, t.int_cell, t.cell_com, t.cell_mass,
+                                            t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
     return cudaGetLastError();
 }
 
 // Capacity of the node arrays for a batched build: exact counts are measured
 // once with a synchronising build and doubled (positions evolve).
 cudaError_t tree_reserve_graph(nb_sim* sim, int n, size_t n_int, size_t n_cells) {
-    NB_TRY(reserve_bodies(sim, pad_up(std::max<size_t>((size_t)n, 1), kSortTile)));
-    NB_TRY(reserve_scan(sim, std::max((size_t)sim->tree.body_cap, (size_t)256 * (sim->tree.body_cap / kSortTile))));
+    const size_t nk = pad_up(std::max<size_t>((size_t)n, 1), kSortTile);
+    NB_TRY(reserve_bodies(sim, nk));
     return reserve_nodes(sim, n_int, n_cells);
 }
 

@@ -429,6 +429,8 @@ def _bind_batch():
         "nb_batch_destroy": ([vp], i32),
         "nb_batch_last_error": ([vp], ctypes.c_char_p),
         "nb_batch_add": ([vp, vp, vp, sz, vp], i32),
+        "nb_batch_add_generated": ([vp, i32, ctypes.c_uint64, sz, vp], i32),
+        "nb_batch_steps_not_run": ([vp, vp], i32),
         "nb_batch_commit": ([vp], i32),
         "nb_batch_set_tuning": ([vp, vp], i32),
         "nb_batch_set_far_field": ([vp, f64], i32),
@@ -501,6 +503,19 @@ class NBodyBatch:
         self._check(lib().nb_batch_add(self._h, _ptr(pm), _ptr(v), pm.shape[0], ctypes.byref(g)), "nb_batch_add")
         self.sizes.append(pm.shape[0])
         return g.value
+
+    def add_generated(self, model: int, seed: int, n: int) -> int:
+        """A galaxy generated on the device at commit: model 0 disk + bulge,
+        1 Plummer sphere, 2 colliding Plummer spheres (the seed_* defaults)."""
+        g = ctypes.c_int32(-1)
+        self._check(lib().nb_batch_add_generated(self._h, model, seed, n, ctypes.byref(g)), "nb_batch_add_generated")
+        self.sizes.append(n)
+        return g.value
+
+    def steps_not_run(self) -> int:
+        v = ctypes.c_int(0)
+        self._check(lib().nb_batch_steps_not_run(self._h, ctypes.byref(v)), "nb_batch_steps_not_run")
+        return v.value
 
     def commit(self):
         self._check(lib().nb_batch_commit(self._h), "nb_batch_commit")

@@ -248,3 +248,22 @@ def test_reinit_same_count_new_tree_shape():
                 assert np.array_equal(out[f], ref[f]), f
             if rec is pairs:
                 assert s.tree_stats()["internal"] > 2 * small["internal"]
+
+
+def test_launches_per_step():
+    """One launch per phase: a plain Barnes-Hut step is at most 20 kernel
+    launches (keys with histograms, sort plan, one per radix pass, gather,
+    positions scan, emit, link, child-count scan, place, mass, traversal,
+    kick-drift)."""
+    import ctypes
+    pm, v = nb.seed_disk(8, 50000)
+    with bh_sim(theta=0.5) as s:
+        s.init_soa(pm, v)
+        s.step(5e-4, 1)
+        s.synchronize()
+        a, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        nb.lib().nb_launch_count(s.handle, ctypes.byref(a))
+        s.step(5e-4, 3)
+        s.synchronize()
+        nb.lib().nb_launch_count(s.handle, ctypes.byref(b))
+    assert (b.value - a.value) / 3 <= 20

@@ -125,6 +125,39 @@ def test_small_counts():
         np.testing.assert_allclose(F, [[6, 0, 0], [-6, 0, 0]], rtol=1e-6)
 
 
+def test_bounded_wait_runs_out_and_handle_recovers():
+    """The force kernel's waits for its source tiles are bounded.  With the
+    budget lowered to zero polls every block gives up at its first tile: the
+    in-flight copies are still waited for, the step is abandoned with the
+    state unchanged, and the next synchronisation reports NB_ETIMEOUT.  With
+    the budget restored the same handle steps to the oracle's result."""
+    pm, v = nb.seed_plummer(21, 65536)
+    rec = nb.records_from_soa(pm, v)
+    with direct_sim() as s:
+        s.init(rec)
+        assert s.get_tune("wait_polls") == 1 << 22
+        s.tune("wait_polls", 0)
+        s.step(1e-3, 1)
+        with pytest.raises(nb.NBodyError) as ei:
+            s.synchronize()
+        assert ei.value.code == nb.NB_ETIMEOUT
+        s.synchronize()                      # the error word was cleared by the report
+        out = rec.copy()
+        s.write_back(out)
+        np.testing.assert_array_equal(out["position"], rec["position"])
+        np.testing.assert_array_equal(out["velocity"], rec["velocity"])
+        s.tune("wait_polls", 1 << 22)
+        s.step(1e-3, 1)
+        s.synchronize()
+        s.write_back(out)
+    # one kick from the initial state: v1 - v0 = F / m dt on sampled bodies
+    sub = np.arange(0, 65536, 64)
+    F = O.direct_forces_subset(rec, sub.astype(np.int32), G=1.0, S=1e-4)
+    dv = out["velocity"][sub] - rec["velocity"][sub]
+    dt = float(np.float32(1e-3))
+    assert O.rel_l2(dv, F / rec["mass"][sub, None] * dt) < FORCE_TOL
+
+
 def test_nonfinite_input_rejected_and_handle_reusable():
     rec = nb.records_from_soa(*nb.seed_plummer(6, 100))
     bad = rec.copy()

@@ -63,16 +63,18 @@ def test_admission_by_memory_budget_and_slots():
 
 
 def test_result_matches_batched_form():
+    """A served job is the batched form's galaxy of the same (model, seed, n),
+    generated on the device, stepped the same number of steps."""
     seed, n, model = JOBS[2]
     with ns.NBodyServer(max_active=4, steps_per_round=4, bh_threshold=8192) as s:
         (i,), _ = run_all(s, [(seed, n, model)], 12)
         pr, vr = s.result(i)
+        assert s.timing()["generate_s"] == 0.0   # nothing of the job was made on the host
         s.release(i)                        # the result is taken: the server forgets the job
         with pytest.raises(nb.NBodyError):
             s.status(i)
-    pm, v = nb.seed_disk(seed, n)
     with nb.NBodyBatch(bh_threshold=8192, bh_theta=0.5, softening2=0.005 ** 2) as b:
-        b.add(pm, v)
+        b.add_generated(model, seed, n)
         b.commit()
         b.step(DT, 12)
         pb, vb = b.read(0)

@@ -62,3 +62,34 @@ def test_noalloc_rejects_sizes_beyond_the_maximum():
     buf = torch.zeros((16, 4), dtype=torch.float32, device="cuda")
     assert fn(buf.data_ptr(), 65537, buf.data_ptr(), 1.0, 1e-4, nb.LAW_REFERENCE, None) == nb.NB_EINVAL
     assert fn(buf.data_ptr(), 0, buf.data_ptr(), 1.0, 1e-4, nb.LAW_REFERENCE, None) == nb.NB_EINVAL
+
+
+def test_noalloc_heavy_masses_then_light():
+    """Masses like the reference's seeders' (up to 1e30, its constants): the
+    self pair must stay exactly zero (no inf * 0 = NaN); the call after it,
+    with N-body masses, matches the handle path again (the shared array's
+    mass record starts from zero on every call)."""
+    import torch
+
+    L = nb.lib()
+    fn = L.nb_direct_accel_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                   ctypes.c_int, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    rec = nb.seed_reference(nb.SEEDER_RANDOM, 23, 3000)
+    heavy = np.zeros((3000, 4), np.float32)
+    heavy[:, :3] = rec["position"]
+    heavy[:, 3] = rec["mass"]
+    G, S = 6.674e-11, 10.0
+    with nb.NBodySim(kind=nb.SIM_BRUTE_FORCE, G=G, softening2=S) as s:
+        s.init_soa(heavy, np.zeros_like(heavy))
+        ref_heavy = s.compute_forces() / heavy[:, 3:4].astype(np.float64)
+    light = nb.seed_plummer(24, 4096)
+    for pm, g, s2, ref in ((heavy, G, S, ref_heavy), (light[0], 1.0, 1e-4, _reference_accel(*light, 0, 1e-4))):
+        d_in = torch.from_numpy(pm).cuda()
+        d_out = torch.full((pm.shape[0], 4), float("nan"), dtype=torch.float32, device="cuda")
+        assert fn(d_in.data_ptr(), pm.shape[0], d_out.data_ptr(), g, s2, nb.LAW_REFERENCE, None) == nb.NB_OK
+        torch.cuda.synchronize()
+        acc = d_out.cpu().numpy()[:, :3].astype(np.float64)
+        assert np.isfinite(acc).all()
+        assert np.linalg.norm(acc - ref) / np.linalg.norm(ref) < FORCE_TOL
