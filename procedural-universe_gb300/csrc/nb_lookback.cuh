@@ -33,9 +33,9 @@ __device__ __forceinline__ unsigned long long lb_load(const unsigned long long* 
 
 // Exclusive prefix of tile `tile` from the status words status[j * stride]
 // of tiles j < tile, read by one thread kLbWindow predecessors at a time (the
-// loads of a window are independent, so a long walk back costs a quarter of
-// the round trips).
-constexpr int kLbWindow = 4;
+// loads of a window are independent and in flight together, so a walk back
+// over many tiles costs 1/kLbWindow of the round trips).
+constexpr int kLbWindow = 16;
 
 __device__ __forceinline__ uint32_t lb_exclusive(const unsigned long long* status, int tile, int stride, int* err) {
     uint32_t sum = 0;
