@@ -283,9 +283,19 @@ int decode_device_error(nb_sim* s) {
     }
 }
 
+// Whether the state's largest mass (h_err[2], read with the error word) needs
+// the direct sum's heavy self-pair guard.
+void note_masses(nb_sim* s) {
+    float m;
+    std::memcpy(&m, &s->h_err[2], sizeof(float));
+    s->heavy = m > 1e21f;
+}
+
 int check_device_error(nb_sim* s) {
     NB_CUDA(s, cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    NB_CUDA(s, cudaMemcpyAsync(s->h_err + 2, s->d_mmax, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
     NB_CUDA(s, cudaStreamSynchronize(s->stream));
+    note_masses(s);
     return decode_device_error(s);
 }
 
@@ -420,7 +430,7 @@ int nb_create(const nb_params* params, nb_sim** out) {
             if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return NB_ECUDA; }
             s->own_stream = true;
         }
-        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 2 * sizeof(int)) != cudaSuccess ||
+        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 4 * sizeof(int)) != cudaSuccess ||
             cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess ||
             cudaMalloc(&s->d_mmax, 2 * sizeof(unsigned)) != cudaSuccess) {
             cudaGetLastError();
@@ -430,7 +440,7 @@ int nb_create(const nb_params* params, nb_sim** out) {
         cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
         cudaMemsetAsync(s->d_inter, 0, sizeof(unsigned long long), s->stream);
         cudaMemsetAsync(s->d_mmax, 0, 2 * sizeof(unsigned), s->stream);
-        s->h_err[0] = s->h_err[1] = 0;
+        s->h_err[0] = s->h_err[1] = s->h_err[2] = s->h_err[3] = 0;
         *out = s;
         return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed
@@ -519,8 +529,13 @@ int init_records(nb_sim* s, const nb_particle* host, int seeder, uint64_t seed, 
     int any = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err + 1, d_any, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->h_err + 2, s->d_mmax, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    if (e == cudaSuccess) any = s->h_err[1];
+    if (e == cudaSuccess) {
+        any = s->h_err[1];
+        note_masses(s);
+    }
     if (e != cudaSuccess) return cuda_fail(s, e, host ? "nb_init_particles" : "nb_init_seeded");
     s->finit_pending = any != 0;
     rc = decode_device_error(s);

@@ -35,14 +35,16 @@ namespace nb {
 // part[splits + split][i] (compensation).  polls bounds each wait for a
 // source tile (kMaxPolls normally; smaller only to test the timeout path);
 // the copies still in flight after a wait gave up are always waited for with
-// the full budget before the block exits.
-template <int LAW, int BLOCK, int IPT, bool COMP>
+// the full budget before the block exits.  HEAVY: the state's largest mass
+// may need more than the law's default self-pair guard (masses above 1e21);
+// the guard is then read from *mmax, else it is the compile-time constant.
+template <int LAW, int BLOCK, int IPT, bool COMP, bool HEAVY>
 __global__ void __launch_bounds__(BLOCK) k_direct_force(const float4* __restrict__ pos, int n_pad,
                                                         int tiles_per_split, int ntiles, int splits, float S,
                                                         float4* __restrict__ part, int* __restrict__ err,
                                                         uint32_t polls, const unsigned* __restrict__ mmax) {
     __shared__ __align__(128) float4 tile[2][kTileJ];
-    const float tiny = self_pair_tiny(mmax);
+    const float tiny = HEAVY ? self_pair_tiny(mmax) : kTiny;
     __shared__ __align__(8) uint64_t bar[2];
 
     const int split = blockIdx.y;
@@ -255,18 +257,22 @@ namespace {
 
 template <int LAW, int BLOCK, int IPT, bool COMP>
 void launch_force_t(dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps, int ntiles, int splits,
-                    float S, float4* part, int* err, uint32_t polls, const unsigned* mmax) {
-    k_direct_force<LAW, BLOCK, IPT, COMP><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S, part, err,
-                                                                 polls, mmax);
+                    float S, float4* part, int* err, uint32_t polls, const unsigned* mmax, bool heavy) {
+    if (heavy)
+        k_direct_force<LAW, BLOCK, IPT, COMP, true><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S, part,
+                                                                           err, polls, mmax);
+    else
+        k_direct_force<LAW, BLOCK, IPT, COMP, false><<<grid, BLOCK, 0, st>>>(pos, n_pad, tps, ntiles, splits, S,
+                                                                            part, err, polls, mmax);
 }
 
 template <int LAW, bool COMP>
 bool launch_force_law(int block, int ipt, dim3 grid, cudaStream_t st, const float4* pos, int n_pad, int tps,
                       int ntiles, int splits, float S, float4* part, int* err, uint32_t polls,
-                      const unsigned* mmax) {
+                      const unsigned* mmax, bool heavy) {
 #define NB_CASE(B, I)                                                                                    \
     if (block == B && ipt == I) {                                                                        \
-        launch_force_t<LAW, B, I, COMP>(grid, st, pos, n_pad, tps, ntiles, splits, S, part, err, polls, mmax); \
+        launch_force_t<LAW, B, I, COMP>(grid, st, pos, n_pad, tps, ntiles, splits, S, part, err, polls, mmax, heavy); \
         return true;                                                                                     \
     }
     NB_CASE(64, 1) NB_CASE(64, 2) NB_CASE(64, 4) NB_CASE(64, 8)
@@ -335,17 +341,17 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     if (sim->prm.law == NB_LAW_PLUMMER)
         ok = comp ? launch_force_law<NB_LAW_PLUMMER, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                           (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                          sim->d_err, sim->wait_polls, sim->d_mmax)
+                                                          sim->d_err, sim->wait_polls, sim->d_mmax, sim->heavy)
                   : launch_force_law<NB_LAW_PLUMMER, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                            (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                           sim->d_err, sim->wait_polls, sim->d_mmax);
+                                                           sim->d_err, sim->wait_polls, sim->d_mmax, sim->heavy);
     else
         ok = comp ? launch_force_law<NB_LAW_REFERENCE, true>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                             (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                            sim->d_err, sim->wait_polls, sim->d_mmax)
+                                                            sim->d_err, sim->wait_polls, sim->d_mmax, sim->heavy)
                   : launch_force_law<NB_LAW_REFERENCE, false>(t.block, t.ipt, grid, sim->stream, sim->pos,
                                                              (int)sim->n_pad, tps, ntiles, splits, S, sim->part,
-                                                             sim->d_err, sim->wait_polls, sim->d_mmax);
+                                                             sim->d_err, sim->wait_polls, sim->d_mmax, sim->heavy);
     }
     if (!ok) return cudaErrorInvalidConfiguration;
     cudaError_t e = cudaGetLastError();
@@ -494,9 +500,9 @@ extern "C" int nb_direct_accel_noalloc(const float* pos_mass4, size_t n, float* 
     const float S = (float)softening2;
     bool ok = law == NB_LAW_PLUMMER
                   ? launch_force_law<NB_LAW_PLUMMER, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles, splits,
-                                                          S, part, err, kMaxPolls, mmax)
+                                                          S, part, err, kMaxPolls, mmax, true)
                   : launch_force_law<NB_LAW_REFERENCE, true>(block, ipt, grid, st, pos, (int)n_pad, tps, ntiles,
-                                                            splits, S, part, err, kMaxPolls, mmax);
+                                                            splits, S, part, err, kMaxPolls, mmax, true);
     if (!ok) return NB_EINVAL;
     k_noalloc_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, (int)n, (int)n_pad, (float)G,
                                                                  reinterpret_cast<float4*>(accel4));

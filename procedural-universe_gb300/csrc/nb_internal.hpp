@@ -174,7 +174,10 @@ struct nb_sim {
     // float bits of the state's largest |mass| (the direct sum's self-pair
     // guard) and of its largest |coordinate|, recorded when a state is loaded
     unsigned* d_mmax = nullptr;
-    int* h_err = nullptr;     // pinned: [0] mirror of d_err, [1] init's non-zero-force flag
+    // the largest mass as last read back: above 1e21 the direct-sum force
+    // kernel takes its self-pair guard from d_mmax (its heavy variant)
+    bool heavy = false;
+    int* h_err = nullptr;     // pinned: [0] mirror of d_err, [1] init's non-zero-force flag, [2..3] of d_mmax
     unsigned long long* d_inter = nullptr;
     uint64_t inter_last = 0;
     bool forces_fresh = false;  // acc holds the forces of the current positions

@@ -35,7 +35,7 @@ __device__ __forceinline__ unsigned long long lb_load(const unsigned long long* 
 // of tiles j < tile, read by one thread kLbWindow predecessors at a time (the
 // loads of a window are independent and in flight together, so a walk back
 // over many tiles costs 1/kLbWindow of the round trips).
-constexpr int kLbWindow = 16;
+constexpr int kLbWindow = 4;
 
 __device__ __forceinline__ uint32_t lb_exclusive(const unsigned long long* status, int tile, int stride, int* err) {
     uint32_t sum = 0;

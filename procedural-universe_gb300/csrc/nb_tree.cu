@@ -50,6 +50,11 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys per tile
+// a radix pass ranks a tile with more threads and fewer keys each (more warps
+// in flight to hide the loads); at most 64 registers, two blocks per SM
+constexpr int kPassThreads = 512;
+constexpr int kPassWarps = kPassThreads / 32;
+constexpr int kPassItems = kSortTile / kPassThreads;
 constexpr int kPasses = 8;
 constexpr int kEmitBlock = 256;
 
@@ -184,7 +189,7 @@ __global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t*
 // Adinets and Merrill 2022): a tile ranks its keys by the pass's digit
 // (warp match_any, warps in order: stable), publishes its digit counts and
 // finds where earlier tiles put theirs by decoupled look-back, then scatters.
-__global__ void __launch_bounds__(kSortThreads) k_sort_pass(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
+__global__ void __launch_bounds__(kPassThreads, 2) k_sort_pass(uint64_t* __restrict__ k0, uint64_t* __restrict__ k1,
                                                             int32_t* __restrict__ v0, int32_t* __restrict__ v1,
                                                             int ntiles, const int32_t* __restrict__ plan, int pass,
                                                             const int32_t* __restrict__ dig_off,
@@ -196,27 +201,27 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(uint64_t* __restrict
     uint64_t* kd = src ? k0 : k1;
     const int32_t* vs = src ? v1 : v0;
     int32_t* vd = src ? v0 : v1;
-    __shared__ uint32_t whist[kSortWarps][256];
+    __shared__ uint32_t whist[kPassWarps][256];
     __shared__ int32_t gbase[256];
     __shared__ int sh_tile;
     const int tile = lb_tile_index(tile_ctr, &sh_tile);
     if (tile >= ntiles) return;   // cannot happen with one block per tile; kept as a guard
-    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&whist[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < kPassWarps * 256; i += kPassThreads) (&whist[0][0])[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int shift = 8 * pass;
-    const int base = tile * kSortTile + warp * (32 * kSortItems) + lane;
-    uint64_t k[kSortItems];
-    int32_t v[kSortItems];
-    uint32_t r[kSortItems];
+    const int base = tile * kSortTile + warp * (32 * kPassItems) + lane;
+    uint64_t k[kPassItems];
+    int32_t v[kPassItems];
+    uint32_t r[kPassItems];
 #pragma unroll
-    for (int it = 0; it < kSortItems; ++it) {
+    for (int it = 0; it < kPassItems; ++it) {
         k[it] = ks[base + it * 32];
         v[it] = vs[base + it * 32];
     }
     const uint32_t lt = lanemask_lt();
 #pragma unroll
-    for (int it = 0; it < kSortItems; ++it) {
+    for (int it = 0; it < kPassItems; ++it) {
         const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const uint32_t b = whist[warp][d];
@@ -226,11 +231,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(uint64_t* __restrict
         __syncwarp();
     }
     __syncthreads();
-    {
+    if (threadIdx.x < 256) {   // one thread per digit
         const int d = threadIdx.x;
         uint32_t run = 0;
 #pragma unroll
-        for (int w = 0; w < kSortWarps; ++w) {
+        for (int w = 0; w < kPassWarps; ++w) {
             const uint32_t c = whist[w][d];
             whist[w][d] = run;
             run += c;
@@ -248,7 +253,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(uint64_t* __restrict
     }
     __syncthreads();
 #pragma unroll
-    for (int it = 0; it < kSortItems; ++it) {
+    for (int it = 0; it < kPassItems; ++it) {
         const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
         const int dst = gbase[d] + (int)whist[warp][d] + (int)r[it];
         kd[dst] = k[it];
@@ -906,7 +911,7 @@ static cudaError_t launch_sort(nb_sim* sim, size_t nk) {
     PhaseScope ps(sim, NB_PHASE_SORT, 1 + kPasses);
     k_sort_plan<<<1, 256, 0, st>>>(t.ghist, (int)nk, t.plan, t.dig_off);
     for (int p = 0; p < kPasses; ++p)
-        k_sort_pass<<<ntiles, kSortThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles, t.plan, p,
+        k_sort_pass<<<ntiles, kPassThreads, 0, st>>>(t.keys[0], t.keys[1], t.vals[0], t.vals[1], ntiles, t.plan, p,
                                                      t.dig_off, t.sort_status + (size_t)p * ntiles * 256,
                                                      t.counters + TC_TILE_SORT + p, sim->d_err);
     return cudaGetLastError();
