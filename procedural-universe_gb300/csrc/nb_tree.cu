@@ -78,7 +78,7 @@ __device__ __forceinline__ uint64_t body_key(const float4 p, float half, int D, 
     uint64_t key = 0;
     float size = __fsub_rn(hi0, lo0);
     for (int l = 0; l < D; ++l) {
-        const float s = __fdiv_rn(size, 2.0f);
+        const float s = __fmul_rn(size, 0.5f);   // Size / 2: exact halving, the same value as a division
         const float m0 = __fadd_rn(lo0, s), m1 = __fadd_rn(lo1, s), m2 = __fadd_rn(lo2, s);
         const float t0 = __fadd_rn(m0, s), t1 = __fadd_rn(m1, s), t2 = __fadd_rn(m2, s);
         int oct = 0;
@@ -337,7 +337,7 @@ __device__ void node_bounds(uint64_t code, int level, float half, float3& lo, fl
     float size = __fsub_rn(hi.x, lo.x);
     for (int l = 1; l <= level; ++l) {
         const int dg = (int)((code >> (3 * (level - l))) & 7ull);
-        const float s = __fdiv_rn(size, 2.0f);
+        const float s = __fmul_rn(size, 0.5f);   // Size / 2: exact halving, the same value as a division
         const float mx = __fadd_rn(lo.x, s), my = __fadd_rn(lo.y, s), mz = __fadd_rn(lo.z, s);
         if (dg & 1) { lo.x = mx; hi.x = __fadd_rn(mx, s); } else { hi.x = mx; }
         if (dg & 2) { lo.y = my; hi.y = __fadd_rn(my, s); } else { hi.y = my; }
