@@ -65,6 +65,14 @@ def batch_galaxies(nb, seed=2024, count=512, lo=256, hi=65536):
 PLAIN_THETAS = (0.5, 0.4, 0.35, 0.3, 0.28, 0.26, 0.24, 0.22, 0.2, 0.18, 0.16)
 
 
+def batched_forces(b, g):
+    """Forces of galaxy g as the batched form's steps see them: after one
+    evaluation, so that the far field's relative rule (which reads the
+    previous accelerations) decides, as it does in every step after the first."""
+    b.forces(g)
+    return b.forces(g)
+
+
 def force_error(nb, F, pm, v, eps2, samples=1024, seed=3):
     """Relative L2 error of forces F against the FP64 direct sum on sampled bodies."""
     n = pm.shape[0]
@@ -110,7 +118,7 @@ def batched_theta_for(nb, pm, v, eps2, thetas, target=1e-3, refine=3):
         with nb.NBodyBatch(bh_threshold=1024, bh_theta=th, softening2=eps2) as b:
             b.add(pm, v)
             b.commit()
-            return force_error(nb, b.forces(0), pm, v, eps2)
+            return force_error(nb, batched_forces(b, 0), pm, v, eps2)
 
     prev = None
     for th in thetas:
@@ -288,7 +296,7 @@ def run_served(args, nb, torch, requests=None, rate=SERVED["rate"], steps=SERVED
     with nb.NBodyBatch(bh_threshold=1024, bh_theta=theta, softening2=eps * eps) as b:
         b.add(pm, v)
         b.commit()
-        served_err = force_error(nb, b.forces(0), pm, v, eps * eps)
+        served_err = force_error(nb, batched_forces(b, 0), pm, v, eps * eps)
     th_eq, err_eq = plain_theta_for(nb, pm, v, eps * eps)
     eq_value, eq_lat = replay(th_eq)
     # the served form at equal accuracy too: its opening angle chosen by the same
@@ -348,7 +356,7 @@ def run_batch_single(args, nb, torch, n=1 << 20, theta=0.5, eps=0.005, dt=5e-4):
         b = nb.NBodyBatch(bh_threshold=1024, bh_theta=th, softening2=eps2, stream=stream.cuda_stream)
         b.add(pm, v)
         b.commit()
-        e = force_error(nb, b.forces(0), pm, v, eps2)
+        e = force_error(nb, batched_forces(b, 0), pm, v, eps2)
         b.step(dt, args.warmup)
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]

@@ -289,11 +289,19 @@ int  nb_batch_add_generated(nb_batch* b, int model, uint64_t seed, size_t n, int
  * buffers. */
 int  nb_batch_commit(nb_batch* b);
 int  nb_batch_set_tuning(nb_batch* b, const nb_tuning* t);
-/* Far field of the group traversal: an accepted cell farther from a group's
- * centre than (group half-diagonal / eta) acts through the group's second-order
- * local expansion instead of once per body.  Default eta = 0.025 / theta^3;
- * 0 evaluates every accepted cell per body. */
+/* Far field of the group traversal: accepted cells far from a group act
+ * through the group's third-order local expansion at its centre instead of
+ * once per body.  Geometric rule (a state's first evaluation, or alpha 0): a
+ * cell farther from the centre than (group half-diagonal / eta) joins it;
+ * default eta = 0.2, 0 turns the rule off. */
 int  nb_batch_set_far_field(nb_batch* b, double eta);
+/* Relative rule of the far field, used once a group's bodies have
+ * accelerations from an earlier evaluation (a previous step, or a previous
+ * batch for a served job): a cell of mass m at distance r joins when
+ * m / r^2 (h / r)^4 < alpha |a|_min / G, h the group's half-diagonal and
+ * |a|_min its bodies' smallest acceleration, and h / r < eta_max.  alpha 0
+ * turns the rule off (the geometric rule decides every evaluation). */
+int  nb_batch_set_far_accuracy(nb_batch* b, double alpha, double eta_max);
 int  nb_batch_get_tuning(nb_batch* b, nb_tuning* t);
 /* Project autotuner: times candidate leaf sizes, then candidate direct-sum
  * tilings, for trial_steps graph replays each (state restored after each
@@ -320,7 +328,9 @@ int  nb_batch_launch_count(nb_batch* b, uint64_t* launches);
 int  nb_batch_tree_stats(nb_batch* b, int64_t* stats4);
 /* Whole-batch state transfer, galaxies in index order concatenated (the sum
  * of their n bodies x float4): upload from / download to host buffers.  A
- * written state may need a larger octree; the next step sizes it. */
+ * written state may need a larger octree; the next step sizes it.  Writing a
+ * state drops the accelerations of the previous one: its first evaluation
+ * takes the far field's geometric rule, as after nb_batch_commit. */
 int  nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4);
 int  nb_batch_read_state(nb_batch* b, float* pos_mass4, float* vel4);
 void* nb_batch_stream(nb_batch* b);

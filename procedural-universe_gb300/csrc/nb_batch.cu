@@ -19,13 +19,19 @@ struct nb_batch {
     nb_params base{};
     size_t bh_threshold = 8192;
     double bh_theta = 0.6;
-    // far-field expansion: an accepted cell farther than (group half-diagonal / far_eta)
-    // from the group's centre acts through the group's local expansion.  The
-    // default far_eta = 0.025 / theta^3 (0.2 at theta 0.5, 0.116 at 0.6) was
-    // calibrated on disk galaxies of 10^4 to 10^6 bodies to add at most ~35% to
-    // the force error of the opening rule itself (2.9e-4 -> 3.8e-4 on the 1M-body
-    // galaxy at theta 0.5); 0 turns it off.
-    double far_eta = 0.0;
+    // Far field of the group traversal (a third-order local expansion at the
+    // group's centre, evaluated once per body).  An accepted cell joins it
+    //  - relative rule, once the group's bodies have accelerations from an
+    //    earlier evaluation: when the cell's truncation-error estimate
+    //    m / r^2 (r_g / r)^4 (r its distance from the centre, r_g the group's
+    //    half-diagonal) is below far_alpha times the group's smallest |a| / G
+    //    and r_g / r < far_cap;
+    //  - geometric rule otherwise (first evaluation of a state, far_alpha 0):
+    //    when r_g / r < far_eta.
+    // far_eta 0 and far_alpha 0 evaluate every accepted cell per body.
+    double far_eta = kFarEta;
+    double far_alpha = kFarAlpha;
+    double far_cap = kFarCap;
     nb_sim* core = nullptr;   // device state of all bodies, stream, error word, tree buffers
     std::string err;
     // galaxies as added
@@ -35,7 +41,7 @@ struct nb_batch {
         size_t off = 0;   // first body in the concatenated arrays
         int idx = -1;     // slot (Barnes-Hut) or direct-galaxy index
         size_t n_pad = 0;
-        const float4* dsrc[4] = {nullptr, nullptr, nullptr, nullptr};   // device source (pos, posc, vel, velc)
+        const float4* dsrc[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // device source (pos, posc, vel, velc, acc)
         int gen_model = -1;      // >= 0: generated on the device at commit (nb_batch_add_generated)
         uint64_t gen_seed = 0;
     };
@@ -166,7 +172,7 @@ bool launch_direct_t(nb_batch* b, int grid, cudaStream_t st, float S) {
 
 // One step (update) or one force evaluation (no update) of every galaxy,
 // enqueued on the core stream without host synchronisation; tree_only stops
-// after the octree topology (enough to read its cell counts).
+// once the octree's node counts are known (no node written).
 int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
     nb_sim* c = b->core;
     cudaStream_t st = c->stream;
@@ -186,7 +192,7 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
                                                                                        b->nslot, b->box_bits);
         }
         NB_BCUDA(b, tree_batch_keys(c, c->pos, b->body_slot, n, b->box_bits, b->nslot, b->gal_box));
-        NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth));
+        NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth, tree_only));
         if (tree_only) return NB_OK;
         {
             PhaseScope ps(c, NB_PHASE_MASS, 3);
@@ -217,6 +223,7 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
         b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, b->cell_walk,     \
         b->cell_q1, b->cell_q2, b->gal_box, b->gal_root, b->nslot,                                                \
         (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, (float)(b->far_eta * b->far_eta),   \
+        (float)(b->far_alpha / b->base.G), (float)(b->far_cap * b->far_cap),                                      \
         100.f * S, c->d_mmax, c->acc, t.interactions, c->d_err)
             if (b->base.law == NB_LAW_PLUMMER) NB_GT(NB_LAW_PLUMMER);
             else NB_GT(NB_LAW_REFERENCE);
@@ -271,28 +278,21 @@ int reserve_tree(nb_batch* b, size_t n_int, size_t n_cells) {
 // Sizes the tree capacity from measured counts (a synchronising force pass).
 int size_tree(nb_batch* b) {
     if (b->n_bh == 0) return NB_OK;
-    size_t gi = 2 * b->n_bh + 64, gc = 3 * b->n_bh + 64;
-    for (int attempt = 0; attempt < 6; ++attempt) {
-        int rc = reserve_tree(b, gi, gc);
-        if (rc) return rc;
-        rc = enqueue_step(b, 0.f, false, true);
-        if (rc) return rc;
-        int32_t h[TC_COUNT];
-        rc = read_tree_counts(b, h);
-        if (rc) return rc;
-        const size_t ni = (size_t)h[TC_NINT], nc = (size_t)h[TC_NINT] + (size_t)h[TC_NLEAF];
-        // the traversal's stack entries carry a cell index below kStackCellLimit
-        if (nc >= (size_t)kStackCellLimit)
-            return bfail(b, NB_EINVAL, "batch too large: its octree needs more than 2^27 cells (about 10^8 "
-                                       "Barnes-Hut bodies); split it over several batches");
-        if (h[TC_OVERFLOW] == 0 && ni <= b->core->tree.int_cap && nc <= b->core->tree.cell_cap) {
-            // room for the tree to grow as the galaxies evolve
-            return reserve_tree(b, 2 * ni + 64, 2 * nc + 64);
-        }
-        gi = std::max(gi * 2, 2 * ni + 64);
-        gc = std::max(gc * 2, 2 * nc + 64);
-    }
-    return bfail(b, NB_ENOMEM, "could not size the batched octree");
+    // the counting pass writes no node: the node arrays need no room yet
+    int rc = reserve_tree(b, 1, 1);
+    if (rc) return rc;
+    rc = enqueue_step(b, 0.f, false, true);
+    if (rc) return rc;
+    int32_t h[TC_COUNT];
+    rc = read_tree_counts(b, h);
+    if (rc) return rc;
+    const size_t ni = (size_t)h[TC_NINT], nc = (size_t)h[TC_NINT] + (size_t)h[TC_NLEAF];
+    // the traversal's stack entries carry a cell index below kStackCellLimit
+    if (nc >= (size_t)kStackCellLimit)
+        return bfail(b, NB_EINVAL, "batch too large: its octree needs more than 2^27 cells (about 10^8 "
+                                   "Barnes-Hut bodies); split it over several batches");
+    // room for the tree to grow as the galaxies evolve
+    return reserve_tree(b, 2 * ni + 64, 2 * nc + 64);
 }
 
 int build_graph(nb_batch* b, float dt) {
@@ -363,8 +363,8 @@ namespace nb {
 // velocity compensation) lives in device memory, e.g. in another batch; the
 // source must stay valid until nb_batch_commit returns.
 int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
-                     size_t n, int32_t* galaxy) {
-    if (!b || !pos || !posc || !vel || !velc || n == 0) return NB_EINVAL;
+                     const float4* acc, size_t n, int32_t* galaxy) {
+    if (!b || !pos || !posc || !vel || !velc || !acc || n == 0) return NB_EINVAL;
     if (b->committed) return bfail(b, NB_EBADSTATE, "galaxies are added before nb_batch_commit");
     if (n > kMaxGalaxyBodies) return bfail(b, NB_EINVAL, "galaxy too large for the batched form");
     b->h_pos.emplace_back();
@@ -372,7 +372,7 @@ int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const f
     nb_batch::Gal g;
     g.n = n;
     g.bh = n >= b->bh_threshold;
-    g.dsrc[0] = pos; g.dsrc[1] = posc; g.dsrc[2] = vel; g.dsrc[3] = velc;
+    g.dsrc[0] = pos; g.dsrc[1] = posc; g.dsrc[2] = vel; g.dsrc[3] = velc; g.dsrc[4] = acc;
     b->gal.push_back(g);
     if (galaxy) *galaxy = (int32_t)(b->gal.size() - 1);
     return NB_OK;
@@ -380,13 +380,14 @@ int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const f
 
 // Device state of a committed galaxy.
 int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,
-                       const float4** velc, size_t* n) {
+                       const float4** velc, const float4** acc, size_t* n) {
     if (!b || !b->committed || galaxy < 0 || (size_t)galaxy >= b->gal.size()) return NB_EINVAL;
     const auto& g = b->gal[(size_t)galaxy];
     *pos = b->core->pos + g.off;
     *posc = b->core->posc + g.off;
     *vel = b->core->vel + g.off;
     *velc = b->core->velc + g.off;
+    *acc = b->core->acc + g.off;
     *n = g.n;
     return NB_OK;
 }
@@ -460,7 +461,6 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
         b->base = p;
         b->bh_threshold = bh_threshold;
         b->bh_theta = bh_theta;
-        b->far_eta = 0.025 / (bh_theta * bh_theta * bh_theta);
         b->core = core;
         if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess || cudaMalloc(&b->held, sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
@@ -623,11 +623,12 @@ int nb_batch_commit(nb_batch* b) {
                 return bfail(b, NB_ENOTSUP, "Barnes-Hut member beyond the float range of the batched form's cell "
                                             "quadrupoles (mass x size^2); use N-body units or the plain path");
         }
-        // galaxies handed over from another batch keep their exact state, compensation included
+        // galaxies handed over from another batch keep their exact state,
+        // compensation and last accelerations included
         for (const auto& g : b->gal) {
             if (!g.dsrc[0]) continue;
-            float4* dst[4] = {b->core->pos, b->core->posc, b->core->vel, b->core->velc};
-            for (int a = 0; a < 4; ++a)
+            float4* dst[5] = {b->core->pos, b->core->posc, b->core->vel, b->core->velc, b->core->acc};
+            for (int a = 0; a < 5; ++a)
                 NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
                                             b->core->stream));
         }
@@ -666,6 +667,20 @@ int nb_batch_set_tuning(nb_batch* b, const nb_tuning* t) {
         if (!b->committed) return NB_OK;
         cudaSetDevice(b->core->dev);
         return plan_units(b);
+    } catch (...) {   // no exception crosses the C-ABI: host allocation failed
+        return NB_ENOMEM;
+    }
+}
+
+int nb_batch_set_far_accuracy(nb_batch* b, double alpha, double eta_max) {
+    try {
+        if (!b) return NB_EINVAL;
+        if (!(alpha >= 0.0) || !(eta_max > 0.0) || eta_max >= 1.0)
+            return bfail(b, NB_EINVAL, "far-field alpha must be >= 0 and eta_max in (0, 1)");
+        b->far_alpha = alpha;
+        b->far_cap = eta_max;
+        b->graph_dirty = true;
+        return NB_OK;
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed
         return NB_ENOMEM;
     }
@@ -827,10 +842,11 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
         nb_sim* c = b->core;
         const size_t bytes = c->n_pad * sizeof(float4);
         float4* save = nullptr;
-        NB_BCUDA(b, cudaMalloc(&save, 4 * bytes));
+        NB_BCUDA(b, cudaMalloc(&save, 5 * bytes));
+        // the state and the accelerations the far field's relative rule reads
         auto snapshot = [&](bool restore) {
-            float4* arrs[4] = {c->pos, c->posc, c->vel, c->velc};
-            for (int k = 0; k < 4; ++k) {
+            float4* arrs[5] = {c->pos, c->posc, c->vel, c->velc, c->acc};
+            for (int k = 0; k < 5; ++k) {
                 if (restore) cudaMemcpyAsync(arrs[k], save + k * c->n_pad, bytes, cudaMemcpyDeviceToDevice, c->stream);
                 else cudaMemcpyAsync(save + k * c->n_pad, arrs[k], bytes, cudaMemcpyDeviceToDevice, c->stream);
             }
@@ -912,6 +928,9 @@ int nb_batch_write_state(nb_batch* b, const float* pos_mass4, const float* vel4)
             NB_BCUDA(b, cudaMemsetAsync(c->velc + g.off, 0, g.n * 16, c->stream));
             src += g.n;
         }
+        // accelerations belong to the previous state: the next evaluation takes
+        // the far field's geometric rule, as after a commit
+        NB_BCUDA(b, cudaMemsetAsync(c->acc, 0, c->n_pad * sizeof(float4), c->stream));
         // validated (reported by the next wait) and the largest mass recorded
         const int rc = sim_rescan_state(c);
         if (rc) return bfail(b, rc, nb_last_error(c));

@@ -43,6 +43,10 @@ constexpr int kGMultiTop = kGStack - 155 - 32;   // stack height up to which a w
 constexpr int kGCells = 64;             // accepted-cell list, per warp
 constexpr int kGBodies = 192;           // gathered leaf-bucket bodies, per warp
 constexpr int kDirTile = 128;           // sources per shared tile of the batched direct kernel
+// far-field defaults of the group traversal (rules in nb_batch.cu's nb_batch)
+constexpr double kFarEta = 0.2;         // geometric rule: group half-diagonal / distance
+constexpr double kFarAlpha = 1e-4;      // relative rule: truncation estimate / (|a|_min / G)
+constexpr double kFarCap = 0.5;         // relative rule: largest half-diagonal / distance
 
 enum : int { BK_SINGLE = 1, BK_BUCKET = 2, BK_INTERNAL = 3 };
 
@@ -222,12 +226,10 @@ __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ counter
         finish_moments(k, int_cell, int_block, int_mask, int_first, spos, cell_com, cell_q1, cell_q2, cell_count,
                        cell_walk, cell_meta, cell_hi, cell_cap, nbodies, err);
         if (k == 0) return;
-        __threadfence();
         const int p = int_parent[k];
         if (p < 0 || p >= ni) return;
-        const int old = atomicAdd(&int_pending[p], 1);
+        const int old = atomic_add_acq_rel(&int_pending[p], 1);   // publishes this node, sees its siblings
         if (old != int_nint[p] - 1) return;
-        __threadfence();
         k = p;
     }
 }
@@ -414,24 +416,31 @@ __device__ __forceinline__ void put_cell(float4 (*lst)[5], int j, float4 cm, flo
 // Far field of a group: accepted cells that are far from the group compared
 // with its size (group half-diagonal < eta * distance from the box centre X)
 // act through a local expansion at X instead of once per body:
-//   a(X + y) = A + J y + 1/2 H(y, y),
+//   a(X + y) = A + J y + 1/2 H(y, y) + 1/6 T(y, y, y),
 // A the cell's full acceleration at X (force law + quadrupole), J the first
-// derivative of its Newtonian monopole + quadrupole field and H the second
-// derivative of the monopole field:
-//   J_ij  = m (3 d_i d_j / r^5 - delta_ij / r^3)
-//         + Q_ij / r^5 - 5 ((Qd)_i d_j + (Qd)_j d_i) / r^7 - 5/2 s delta_ij / r^7 + 35/2 s d_i d_j / r^9,
-//   H_ijk = m (15 d_i d_j d_k / r^7 - 3 (delta_ik d_j + delta_jk d_i + delta_ij d_k) / r^5),
-// d = COM - X, s = d.Q.d (the quadrupole part of J is minus the derivative,
-// with respect to d, of the quadrupole acceleration -Q d / r^5 + 5/2 s d / r^7).
-// H is fully symmetric: xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz.
-constexpr int kFarTerms = 19;   // A (3), J (6: xx yy zz xy xz yz), H (10)
+// derivative of its Newtonian monopole + quadrupole field, H and T the second
+// and third derivatives of the monopole field (with d = COM - X, r = |d|,
+// s = d.Q.d):
+//   J_ij   = m (3 d_i d_j / r^5 - delta_ij / r^3)
+//          + Q_ij / r^5 - 5 ((Qd)_i d_j + (Qd)_j d_i) / r^7 - 5/2 s delta_ij / r^7 + 35/2 s d_i d_j / r^9,
+//   H_ijk  = m (15 d_i d_j d_k / r^7 - 3 (delta_ik d_j + delta_jk d_i + delta_ij d_k) / r^5),
+//   T_ijkl = m (105 d_i d_j d_k d_l / r^9 - 15 (delta_ij d_k d_l + 5 more pairings) / r^7
+//               + 3 (delta_ij delta_kl + delta_ik delta_jl + delta_il delta_jk) / r^5)
+// (the quadrupole part of J is minus the derivative, with respect to d, of
+// the quadrupole acceleration -Q d / r^5 + 5/2 s d / r^7).  Each is a
+// derivative tensor of a harmonic potential, so every trace vanishes and only
+// the independent components are summed: J 5 (zz = -xx - yy), H 7 (xzz, yzz,
+// zzz from the traces), T 9 (xxzz, yyzz, zzzz, xyzz, xzzz, yzzz from the
+// traces).  The truncation error of a cell's term falls as (size / distance)^4.
+constexpr int kFarTerms = 24;   // A (3), J xx yy xy xz yz (5), H (7), T (9)
 struct FarField {
     float v[kFarTerms];
 };
 
+// Adds one cell's terms to a lane's partial sums (term k at f[k * stride]).
 template <int LAW>
-__device__ __forceinline__ void far_add(FarField& f, const float4 cm, const float4 q1, const float4 q2, float Xx,
-                                        float Xy, float Xz, float S) {
+__device__ __forceinline__ void far_add(float* f, int stride, const float4 cm, const float4 q1, const float4 q2,
+                                        float Xx, float Xy, float Xz, float S) {
     const float dx = cm.x - Xx, dy = cm.y - Xy, dz = cm.z - Xz;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const float m = cm.w;
@@ -450,44 +459,63 @@ __device__ __forceinline__ void far_add(FarField& f, const float4 cm, const floa
     const float qz = fmaf(q2.y, dx, fmaf(q2.z, dy, q1.z * dz));
     const float sq = fmaf(dx, qx, fmaf(dy, qy, dz * qz));   // d.Q.d
     const float c7 = 2.5f * sq * ir7;
-    float* v = f.v;
-    v[0] += fmaf(w + c7, dx, -qx * ir5);
-    v[1] += fmaf(w + c7, dy, -qy * ir5);
-    v[2] += fmaf(w + c7, dz, -qz * ir5);
+    f[0 * stride] += fmaf(w + c7, dx, -qx * ir5);
+    f[1 * stride] += fmaf(w + c7, dy, -qy * ir5);
+    f[2 * stride] += fmaf(w + c7, dz, -qz * ir5);
     const float m3 = 3.f * m * ir5, m1 = m * ir3;
     const float t5 = 5.f * ir7, g9 = 17.5f * sq * ir7 * ir2, dg = m1 + c7;   // c7 = 5/2 s / r^7
-    v[3] += fmaf(m3 * dx, dx, -dg) + fmaf(q1.x, ir5, dx * fmaf(g9, dx, -2.f * t5 * qx));   // J xx
-    v[4] += fmaf(m3 * dy, dy, -dg) + fmaf(q1.y, ir5, dy * fmaf(g9, dy, -2.f * t5 * qy));   // J yy
-    v[5] += fmaf(m3 * dz, dz, -dg) + fmaf(q1.z, ir5, dz * fmaf(g9, dz, -2.f * t5 * qz));   // J zz
-    v[6] += fmaf(m3 * dx + g9 * dx, dy, fmaf(q2.x, ir5, -t5 * fmaf(qx, dy, qy * dx)));     // J xy
-    v[7] += fmaf(m3 * dx + g9 * dx, dz, fmaf(q2.y, ir5, -t5 * fmaf(qx, dz, qz * dx)));     // J xz
-    v[8] += fmaf(m3 * dy + g9 * dy, dz, fmaf(q2.z, ir5, -t5 * fmaf(qy, dz, qz * dy)));     // J yz
+    f[3 * stride] += fmaf(m3 * dx, dx, -dg) + fmaf(q1.x, ir5, dx * fmaf(g9, dx, -2.f * t5 * qx));   // J xx
+    f[4 * stride] += fmaf(m3 * dy, dy, -dg) + fmaf(q1.y, ir5, dy * fmaf(g9, dy, -2.f * t5 * qy));   // J yy
+    f[5 * stride] += fmaf(m3 * dx + g9 * dx, dy, fmaf(q2.x, ir5, -t5 * fmaf(qx, dy, qy * dx)));     // J xy
+    f[6 * stride] += fmaf(m3 * dx + g9 * dx, dz, fmaf(q2.y, ir5, -t5 * fmaf(qx, dz, qz * dx)));     // J xz
+    f[7 * stride] += fmaf(m3 * dy + g9 * dy, dz, fmaf(q2.z, ir5, -t5 * fmaf(qy, dz, qz * dy)));     // J yz
     const float m15 = 15.f * m * ir7;
-    const float tx = m15 * dx, ty = m15 * dy, tz = m15 * dz;
-    v[9] += dx * fmaf(tx, dx, -3.f * m3);    // H xxx = 15 m dx^3 / r^7 - 9 m dx / r^5
-    v[10] += dy * fmaf(ty, dy, -3.f * m3);   // H yyy
-    v[11] += dz * fmaf(tz, dz, -3.f * m3);   // H zzz
-    v[12] += dy * fmaf(tx, dx, -m3);         // H xxy
-    v[13] += dz * fmaf(tx, dx, -m3);         // H xxz
-    v[14] += dx * fmaf(ty, dy, -m3);         // H xyy
-    v[15] += dz * fmaf(ty, dy, -m3);         // H yyz
-    v[16] += dx * fmaf(tz, dz, -m3);         // H xzz
-    v[17] += dy * fmaf(tz, dz, -m3);         // H yzz
-    v[18] += tx * dy * dz;                   // H xyz
+    const float tx = m15 * dx, ty = m15 * dy;
+    f[8 * stride] += dx * fmaf(tx, dx, -3.f * m3);    // H xxx = 15 m dx^3 / r^7 - 9 m dx / r^5
+    f[9 * stride] += dy * fmaf(ty, dy, -3.f * m3);    // H yyy
+    f[10 * stride] += dy * fmaf(tx, dx, -m3);         // H xxy
+    f[11 * stride] += dz * fmaf(tx, dx, -m3);         // H xxz
+    f[12 * stride] += dx * fmaf(ty, dy, -m3);         // H xyy
+    f[13 * stride] += dz * fmaf(ty, dy, -m3);         // H yyz
+    f[14 * stride] += tx * dy * dz;                   // H xyz
+    const float a9 = 105.f * m * ir7 * ir2;           // 105 m / r^9
+    const float x2 = dx * dx, y2 = dy * dy;
+    const float ax2 = a9 * x2, ay2 = a9 * y2;
+    f[15 * stride] += fmaf(x2, ax2 - 6.f * m15, 3.f * m3);          // T xxxx
+    f[16 * stride] += fmaf(y2, ay2 - 6.f * m15, 3.f * m3);          // T yyyy
+    f[17 * stride] += fmaf(ax2, y2, fmaf(-m15, x2 + y2, m3));        // T xxyy
+    f[18 * stride] += dx * dy * (ax2 - 3.f * m15);                  // T xxxy
+    f[19 * stride] += dx * dy * (ay2 - 3.f * m15);                  // T xyyy
+    f[20 * stride] += dx * dz * (ax2 - 3.f * m15);                  // T xxxz
+    f[21 * stride] += dx * dz * (ay2 - m15);                        // T xyyz
+    f[22 * stride] += dy * dz * (ax2 - m15);                        // T xxyz
+    f[23 * stride] += dy * dz * (ay2 - 3.f * m15);                  // T yyyz
 }
 
-// A + J y + 1/2 H(y, y) at offset y from the expansion centre.
-__device__ __forceinline__ void far_eval(const FarField& f, float yx, float yy, float yz, float& ax, float& ay,
+// A + J y + 1/2 H(y, y) + 1/6 T(y, y, y) at offset y from the expansion centre.
+__device__ __forceinline__ void far_eval(const FarField& f, float x, float y, float z, float& ax, float& ay,
                                          float& az) {
     const float* v = f.v;
-    const float* h = v + 9;   // xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz
-    const float xx = yx * yx, yy2 = yy * yy, zz = yz * yz, xy = yx * yy, xz = yx * yz, yz2 = yy * yz;
-    ax = v[0] + v[3] * yx + v[6] * yy + v[7] * yz +
-         0.5f * (h[0] * xx + h[5] * yy2 + h[7] * zz) + h[3] * xy + h[4] * xz + h[9] * yz2;
-    ay = v[1] + v[6] * yx + v[4] * yy + v[8] * yz +
-         0.5f * (h[3] * xx + h[1] * yy2 + h[8] * zz) + h[5] * xy + h[9] * xz + h[6] * yz2;
-    az = v[2] + v[7] * yx + v[8] * yy + v[5] * yz +
-         0.5f * (h[4] * xx + h[6] * yy2 + h[2] * zz) + h[9] * xy + h[7] * xz + h[8] * yz2;
+    const float Jxx = v[3], Jyy = v[4], Jxy = v[5], Jxz = v[6], Jyz = v[7], Jzz = -Jxx - Jyy;
+    const float Hxxx = v[8], Hyyy = v[9], Hxxy = v[10], Hxxz = v[11], Hxyy = v[12], Hyyz = v[13], Hxyz = v[14];
+    const float Hxzz = -Hxxx - Hxyy, Hyzz = -Hxxy - Hyyy, Hzzz = -Hxxz - Hyyz;
+    const float Txxxx = v[15], Tyyyy = v[16], Txxyy = v[17], Txxxy = v[18], Txyyy = v[19], Txxxz = v[20],
+                Txyyz = v[21], Txxyz = v[22], Tyyyz = v[23];
+    const float Txxzz = -Txxxx - Txxyy, Tyyzz = -Txxyy - Tyyyy, Tzzzz = -Txxzz - Tyyzz;
+    const float Txyzz = -Txxxy - Txyyy, Txzzz = -Txxxz - Txyyz, Tyzzz = -Txxyz - Tyyyz;
+    const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
+    const float x3 = xx * x, y3 = yy * y, z3 = zz * z;
+    const float x2y = xx * y, x2z = xx * z, xy2 = x * yy, y2z = yy * z, xz2 = x * zz, yz2 = y * zz, xyz = xy * z;
+    constexpr float s6 = 1.f / 6.f;
+    ax = v[0] + Jxx * x + Jxy * y + Jxz * z + 0.5f * (Hxxx * xx + Hxyy * yy + Hxzz * zz) + Hxxy * xy + Hxxz * xz +
+         Hxyz * yz + s6 * (Txxxx * x3 + Txyyy * y3 + Txzzz * z3) +
+         0.5f * (Txxxy * x2y + Txxxz * x2z + Txxyy * xy2 + Txxzz * xz2 + Txyyz * y2z + Txyzz * yz2) + Txxyz * xyz;
+    ay = v[1] + Jxy * x + Jyy * y + Jyz * z + 0.5f * (Hxxy * xx + Hyyy * yy + Hyzz * zz) + Hxyy * xy + Hxyz * xz +
+         Hyyz * yz + s6 * (Txxxy * x3 + Tyyyy * y3 + Tyzzz * z3) +
+         0.5f * (Txxyy * x2y + Txxyz * x2z + Txyyy * xy2 + Txyzz * xz2 + Tyyyz * y2z + Tyyzz * yz2) + Txyyz * xyz;
+    az = v[2] + Jxz * x + Jyz * y + Jzz * z + 0.5f * (Hxxz * xx + Hyyz * yy + Hzzz * zz) + Hxyz * xy + Hxzz * xz +
+         Hyzz * yz + s6 * (Txxxz * x3 + Tyyyz * y3 + Tzzzz * z3) +
+         0.5f * (Txxyz * x2y + Txxzz * x2z + Txyyz * xy2 + Txzzz * xz2 + Tyyzz * y2z + Tyzzz * yz2) + Txyzz * xyz;
 }
 
 // Persistent: each warp takes groups from the queue until it is empty.
@@ -497,7 +525,8 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const float4* __restrict__ cell_com,
     const int4* __restrict__ cell_walk, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
     const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
-    int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_min_r2,
+    int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_rel, float far_cap2,
+    float far_min_r2,
     const unsigned* __restrict__ mmax, float4* __restrict__ acc,
     unsigned long long* __restrict__ inter, int* __restrict__ err) {
     __shared__ int stk[kGWarps][kGStack];
@@ -543,6 +572,23 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const float Xx = 0.5f * (bl[0] + bh[0]), Xy = 0.5f * (bl[1] + bh[1]), Xz = 0.5f * (bl[2] + bh[2]);
     const float rg2 = 0.25f * ((bh[0] - bl[0]) * (bh[0] - bl[0]) + (bh[1] - bl[1]) * (bh[1] - bl[1]) +
                                (bh[2] - bl[2]) * (bh[2] - bl[2]));
+    // relative far-field rule: the group's smallest |a| / G of the previous
+    // evaluation (none yet: 0, the geometric rule decides)
+    float far_thr = 0.f;
+    if (far_rel > 0.f) {
+        float a2 = INFINITY;
+        if (v0) {
+            const float4 a = acc[sorder[s0]];
+            a2 = fmaf(a.z, a.z, fmaf(a.y, a.y, a.x * a.x));
+        }
+        if (v1) {
+            const float4 a = acc[sorder[s1]];
+            a2 = fminf(a2, fmaf(a.z, a.z, fmaf(a.y, a.y, a.x * a.x)));
+        }
+        for (int o = 16; o > 0; o >>= 1) a2 = fminf(a2, __shfl_xor_sync(0xffffffffu, a2, o));
+        if (a2 > 0.f && a2 < INFINITY) far_thr = far_rel * sqrtf(a2);
+    }
+    const bool use_far = far2 > 0.f || far_rel > 0.f;
     for (int k = 0; k < kFarTerms; ++k) ffs[w][k][lane] = 0.f;   // this lane's share of the far field
     // negated target coordinates, duplicated: the pair partner is the other list entry
     const float2 n0x = make_float2(-p0.x, -p0.x), n0y = make_float2(-p0.y, -p0.y), n0z = make_float2(-p0.z, -p0.z);
@@ -726,14 +772,18 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             a_cell = accept && count > 2 && kind == BK_INTERNAL;
             a_range = !a_cell && (count <= leaf_size || kind != BK_INTERNAL);
             a_push = !a_cell && !a_range;
-            if (a_cell && far2 > 0.f) {
+            if (a_cell && use_far) {
                 const float ex = ccm.x - Xx, ey = ccm.y - Xy, ez = ccm.z - Xz;
                 const float r2X = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
-                if (rg2 < far2 * r2X && r2X > far_min_r2) {   // far: into the group's local expansion
-                    FarField t;
-                    for (int k = 0; k < kFarTerms; ++k) t.v[k] = 0.f;
-                    far_add<LAW>(t, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]), Xx, Xy, Xz, S);
-                    for (int k = 0; k < kFarTerms; ++k) ffs[w][k][lane] += t.v[k];
+                bool far;
+                if (far_thr > 0.f) {   // m / r^2 (r_g / r)^4 < alpha |a|_min / G, r_g / r < cap
+                    const float q = rg2 / r2X;
+                    far = rg2 < far_cap2 * r2X && ccm.w * q * q < far_thr * r2X;
+                } else {
+                    far = rg2 < far2 * r2X;
+                }
+                if (far && r2X > far_min_r2) {   // far: into the group's local expansion
+                    far_add<LAW>(&ffs[w][0][lane], 32, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]), Xx, Xy, Xz, S);
                     cnt += (unsigned)grp.z;
                     a_cell = false;   // accepted, not listed
                 }
@@ -769,7 +819,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     }
     fold();
     // the group's far field: sum the lanes' partial expansions, evaluate at each body
-    if (far2 > 0.f) {
+    if (use_far) {
         FarField ff;
         for (int k = 0; k < kFarTerms; ++k) {
             float x = ffs[w][k][lane];

@@ -75,6 +75,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // Hardware approximate reciprocal square root (MUFU.RSQ), flush-to-zero.
+// atomicAdd with acquire-release semantics at GPU scope: the caller's earlier
+// writes are visible to whoever later acquires this location, and the
+// caller sees the writes released to it by earlier adders (the bottom-up
+// tree passes: the last child to arrive reads its siblings' results).
+__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ float rsqrt_approx(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));

@@ -219,7 +219,9 @@ cudaError_t tree_forces(nb_sim* sim);
 cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal);
 float theta_float(double theta);   // smallest float >= theta
 // Batched form: topology of pre-computed keys without host synchronisation.
-cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D);
+// counts_only: stop once the node counts are known (no node is written, so
+// the node arrays may still be too small for the tree).
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only = false);
 // Words of the counters buffer (counters, tile counters, radix histograms)
 // that a batched step clears before its keys.
 int tree_counter_words();
@@ -243,10 +245,12 @@ int sim_rescan_state(nb_sim* s);
 
 // ---- batched form hand-over (nb_batch.cu), used by the served form ----
 constexpr size_t kMaxGalaxyBodies = (size_t)1 << 24;   // bodies of one galaxy in the batched form
+// A galaxy handed over keeps its state, its compensation terms and its last
+// accelerations (the relative far-field rule of the next step reads them).
 int batch_add_device(nb_batch* b, const float4* pos, const float4* posc, const float4* vel, const float4* velc,
-                     size_t n, int32_t* galaxy);
+                     const float4* acc, size_t n, int32_t* galaxy);
 int batch_device_state(nb_batch* b, int32_t galaxy, const float4** pos, const float4** posc, const float4** vel,
-                       const float4** velc, size_t* n);
+                       const float4** velc, const float4** acc, size_t* n);
 // nb_batch_step in two halves: enqueue the steps, then wait for them and check
 // the device's error and overflow flags.
 int batch_launch_steps(nb_batch* b, float dt, int nsteps);

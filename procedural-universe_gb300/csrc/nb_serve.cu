@@ -90,10 +90,10 @@ int rebuild(nb_server* s) {
         const Job& j = s->jobs[s->active[a]];
         int32_t g = -1;
         if (j.galaxy >= 0 && s->batch) {
-            const float4 *p, *pc, *v, *vc;
+            const float4 *p, *pc, *v, *vc, *ac;
             size_t n = 0;
-            rc = batch_device_state(s->batch, j.galaxy, &p, &pc, &v, &vc, &n);
-            if (!rc) rc = batch_add_device(nb2, p, pc, v, vc, n, &g);
+            rc = batch_device_state(s->batch, j.galaxy, &p, &pc, &v, &vc, &ac, &n);
+            if (!rc) rc = batch_add_device(nb2, p, pc, v, vc, ac, n, &g);
         } else {
             rc = nb_batch_add_generated(nb2, j.spec.model, j.spec.seed, j.spec.n, &g);
         }

@@ -731,11 +731,9 @@ __global__ void k_mass(int n_int, const int32_t* __restrict__ n_int_dev, const i
     for (int guard = 0; guard < 64; ++guard) {   // a path has at most 22 internal nodes
         finish_node(k, int_cell, int_block, int_mask, cell_com, cell_mass, cell_count, dropped);
         if (k == 0) return;
-        __threadfence();
         const int p = int_parent[k];
-        const int old = atomicAdd(&int_pending[p], 1);
+        const int old = atomic_add_acq_rel(&int_pending[p], 1);   // publishes this node, sees its siblings
         if (old != int_nint[p] - 1) return;
-        __threadfence();
         k = p;
     }
 }
@@ -1026,7 +1024,7 @@ cudaError_t tree_batch_keys(nb_sim* sim, const float4* pos, const int32_t* body_
     return cudaGetLastError();
 }
 
-cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only) {
     TreeBuffers& t = sim->tree;
     const size_t nk = pad_up(std::max<size_t>((size_t)n, 1), kSortTile);
     const int ntiles = (int)(nk / kSortTile);
@@ -1053,7 +1051,9 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D) {
                                                     t.spos);
     // this scan also clears the internal-node hash table for the emission
     k_positions_scan<<<ntiles, kSortThreads, 0, st>>>(tv, t.spos, t.pos_nint, t.leaf_level, t.leaf_count, t.counters,
-                                                      t.pos_status, ntiles, t.hkeys, (int)t.hash_cap, sim->d_err);
+                                                      t.pos_status, ntiles, counts_only ? nullptr : t.hkeys,
+                                                      (int)t.hash_cap, sim->d_err);
+    if (counts_only) return cudaGetLastError();   // the node counts are in counters[TC_NINT], [TC_NLEAF]
     k_emit<<<nbk, kEmitBlock, 0, st>>>(tv, t.pos_nint, t.int_level, t.int_first, t.int_code, t.hkeys, t.hvals, hmask,
                                       t.int_mask, t.int_nint, t.int_pending, t.counters, t.popc_status, ptiles);
     k_link<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_first, t.int_code, tv, icap, t.counters + TC_NINT, ib,

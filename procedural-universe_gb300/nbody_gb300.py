@@ -434,6 +434,7 @@ def _bind_batch():
         "nb_batch_commit": ([vp], i32),
         "nb_batch_set_tuning": ([vp, vp], i32),
         "nb_batch_set_far_field": ([vp, f64], i32),
+        "nb_batch_set_far_accuracy": ([vp, f64, f64], i32),
         "nb_batch_get_tuning": ([vp, vp], i32),
         "nb_batch_autotune": ([vp, f32, i32], i32),
         "nb_batch_step": ([vp, f32, i32], i32),
@@ -540,6 +541,9 @@ class NBodyBatch:
 
     def set_far_field(self, eta: float):
         self._check(lib().nb_batch_set_far_field(self._h, eta), "nb_batch_set_far_field")
+
+    def set_far_accuracy(self, alpha: float, eta_max: float = 0.5):
+        self._check(lib().nb_batch_set_far_accuracy(self._h, alpha, eta_max), "nb_batch_set_far_accuracy")
 
     def read(self, g):
         n = self.sizes[g]

@@ -143,7 +143,8 @@ def test_coincident_bodies_and_far_field():
     """A Plummer sphere with 150 bodies on one point: the coincident bodies end
     in a depth-cap bucket larger than a traversal group (cut into chunks, and
     summed body by body where it is opened); the far field's local expansion
-    is on by default and off with eta = 0, both within the error bound."""
+    is on by default and off with eta = 0 and alpha = 0, both within the
+    error bound."""
     pm, v = nb.seed_plummer(21, 20000)
     clump = np.tile(np.array([[0.3, -0.2, 0.1, pm[0, 3]]], np.float32), (150, 1))
     pm = np.concatenate([pm, clump]).astype(np.float32)
@@ -154,12 +155,38 @@ def test_coincident_bodies_and_far_field():
     with make_batch([(pm, v)]) as b:
         F_far = b.forces(0)
         b.set_far_field(0.0)
+        b.set_far_accuracy(0.0)
         F_near = b.forces(0)
         assert b.info()["interactions"] > 0
     assert np.all(np.isfinite(F_far)) and np.all(np.isfinite(F_near))
     assert O.rel_l2(F_far[t], ref) < BH_FP64_TOL
     assert O.rel_l2(F_near[t], ref) < BH_FP64_TOL
     assert not np.array_equal(F_far, F_near)   # the expansion was used
+
+
+def test_far_field_relative_rule():
+    """A state's first evaluation takes the geometric far-field rule; later
+    ones (accelerations known) the relative rule, which must differ from it
+    and stay within the error bound at the workload's theta for galaxies of
+    4,096 to 200,000 bodies.  alpha 0 keeps the geometric rule (the second
+    evaluation then repeats the first bit for bit); bad values are refused."""
+    for pm, v in (nb.seed_disk(91, 4096), nb.seed_plummer(77, 65536), nb.seed_disk(5, 200_000)):
+        n = pm.shape[0]
+        t = np.arange(0, n, max(1, n // 1024)).astype(np.int32)
+        ref = fp64_forces(pm, v, t)
+        with nb.NBodyBatch(bh_threshold=1024, bh_theta=0.5, softening2=EPS2) as b:
+            b.add(pm, v)
+            b.commit()
+            F_geo = b.forces(0)
+            F_rel = b.forces(0)
+            assert not np.array_equal(F_geo, F_rel)
+            assert O.rel_l2(F_geo[t], ref) < BH_FP64_TOL, n
+            assert O.rel_l2(F_rel[t], ref) < BH_FP64_TOL, n
+            b.set_far_accuracy(0.0)
+            np.testing.assert_array_equal(b.forces(0), F_geo)
+            for bad in ((-1.0, 0.5), (1e-4, 0.0), (1e-4, 1.0)):
+                with pytest.raises(nb.NBodyError):
+                    b.set_far_accuracy(*bad)
 
 
 def test_ragged_galaxy_sizes():
