@@ -16,6 +16,9 @@
 #include <thread>
 #include <vector>
 #include <algorithm>
+#include <cstdint>
+#include <map>
+#include <mutex>
 
 using namespace nb;
 
@@ -193,10 +196,10 @@ bool host_direct(const nb_sim* s) { return s->pageable_access == 1 && !(s->prm.f
 void* device_stage(nb_sim* s, size_t bytes) {
     if (bytes > s->d_stage_bytes) {
         cudaStreamSynchronize(s->stream);
-        cudaFree(s->d_stage);
+        dev_free(s->d_stage, s->stream);
         s->d_stage = nullptr;
         s->d_stage_bytes = 0;
-        if (cudaMalloc(&s->d_stage, bytes) != cudaSuccess) {
+        if (dev_alloc(&s->d_stage, bytes) != cudaSuccess) {
             cudaGetLastError();
             s->d_stage = nullptr;
             return nullptr;
@@ -231,8 +234,9 @@ void detach_render(nb_sim* s) {
 
 void free_state(nb_sim* s) {
     detach_render(s);
-    cudaFree(s->pos); cudaFree(s->posc); cudaFree(s->vel); cudaFree(s->velc); cudaFree(s->acc);
-    cudaFree(s->finit); cudaFree(s->part);
+    for (void* p : {(void*)s->pos, (void*)s->posc, (void*)s->vel, (void*)s->velc, (void*)s->acc, (void*)s->finit,
+                    (void*)s->part})
+        dev_free(p, s->stream);
     s->pos = s->posc = s->vel = s->velc = s->acc = s->finit = s->part = nullptr;
     s->part_cap = 0;
     s->cap = 0;
@@ -247,7 +251,7 @@ int ensure_state(nb_sim* s, size_t n) {
         const size_t bytes = n_pad * sizeof(float4);
         float4** arrs[] = {&s->pos, &s->posc, &s->vel, &s->velc, &s->acc, &s->finit};
         for (float4** a : arrs) {
-            cudaError_t e = cudaMalloc(a, bytes);
+            cudaError_t e = dev_alloc(a, bytes);
             if (e != cudaSuccess) {
                 free_state(s);
                 cudaGetLastError();
@@ -334,6 +338,52 @@ bool params_valid(const nb_params* p, std::string& why) {
 }  // namespace
 
 namespace nb {
+
+struct DevicePool {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t stream = nullptr;   // allocations are ordered on it, then waited for
+};
+static std::mutex g_pool_mu;
+static std::map<int, DevicePool> g_pools;
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    DevicePool& P = g_pools[dev];
+    if (!P.pool) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        e = cudaMemPoolCreate(&P.pool, &props);
+        if (e != cudaSuccess) { P.pool = nullptr; return e; }
+        // keep freed memory in the pool for the next allocation
+        uint64_t keep = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(P.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(P.pool);
+            P.pool = nullptr;
+            P.stream = nullptr;
+            return e;
+        }
+    }
+    e = cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 1), P.pool, P.stream);
+    if (e != cudaSuccess) { *p = nullptr; return e; }
+    // the allocation has taken place in stream order: usable on every stream
+    e = cudaStreamSynchronize(P.stream);
+    if (e != cudaSuccess) { cudaFreeAsync(*p, P.stream); *p = nullptr; }
+    return e;
+}
+
+void dev_free(void* p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+}
+
 
 int sim_reserve_zeroed(nb_sim* s, size_t n) {
     if (n > (size_t)INT32_MAX - kPad) return fail(s, NB_EINVAL, "too many particles");
@@ -430,9 +480,9 @@ int nb_create(const nb_params* params, nb_sim** out) {
             if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) { delete s; return NB_ECUDA; }
             s->own_stream = true;
         }
-        if (cudaMalloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 4 * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess ||
-            cudaMalloc(&s->d_mmax, 2 * sizeof(unsigned)) != cudaSuccess) {
+        if (dev_alloc(&s->d_err, sizeof(int)) != cudaSuccess || cudaMallocHost(&s->h_err, 4 * sizeof(int)) != cudaSuccess ||
+            dev_alloc(&s->d_inter, sizeof(unsigned long long)) != cudaSuccess ||
+            dev_alloc(&s->d_mmax, 2 * sizeof(unsigned)) != cudaSuccess) {
             cudaGetLastError();
             nb_destroy(s);
             return NB_ENOMEM;
@@ -454,14 +504,14 @@ int nb_destroy(nb_sim* s) {
         cudaSetDevice(s->dev);
         if (s->stream) cudaStreamSynchronize(s->stream);
         free_state(s);
-        cudaFree(s->d_stage);
+        dev_free(s->d_stage, s->stream);
         if (s->h_stage) cudaFreeHost(s->h_stage);
         for (auto& p : s->prof.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (cudaEvent_t e : s->prof.pool) cudaEventDestroy(e);
-        cudaFree(s->dscratch);
-        cudaFree(s->d_err);
-        cudaFree(s->d_inter);
-        cudaFree(s->d_mmax);
+        dev_free(s->dscratch, s->stream);
+        dev_free(s->d_err, s->stream);
+        dev_free(s->d_inter, s->stream);
+        dev_free(s->d_mmax, s->stream);
         if (s->h_err) cudaFreeHost(s->h_err);
         if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
         delete s;

@@ -101,11 +101,11 @@ int bfail(nb_batch* b, int code, const std::string& msg) {
     } while (0)
 
 template <typename T>
-cudaError_t upload(T** dst, const std::vector<T>& src) {
-    if (*dst) cudaFree(*dst);
+cudaError_t upload(T** dst, const std::vector<T>& src, cudaStream_t st) {
+    dev_free(*dst, st);
     *dst = nullptr;
     if (src.empty()) return cudaSuccess;
-    cudaError_t e = cudaMalloc(dst, src.size() * sizeof(T));
+    cudaError_t e = dev_alloc(dst, src.size() * sizeof(T));
     if (e != cudaSuccess) return e;
     return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
@@ -141,15 +141,15 @@ int plan_units(nb_batch* b) {
         part_base += 2 * (size_t)splits * g.n_pad;
     }
     if (part_base > (size_t)INT32_MAX) return bfail(b, NB_ENOMEM, "direct-sum partials exceed 2^31 entries");
-    NB_BCUDA(b, upload(&b->units, units));
-    NB_BCUDA(b, upload(&b->unit_comp, ucomp));
-    NB_BCUDA(b, upload(&b->dgal, dg));
+    NB_BCUDA(b, upload(&b->units, units, b->core->stream));
+    NB_BCUDA(b, upload(&b->unit_comp, ucomp, b->core->stream));
+    NB_BCUDA(b, upload(&b->dgal, dg, b->core->stream));
     b->nunits = (int)units.size();
     if (part_base > b->part_cap) {
-        cudaFree(b->part);
+        dev_free(b->part, b->core->stream);
         b->part = nullptr;
         b->part_cap = 0;
-        NB_BCUDA(b, cudaMalloc(&b->part, std::max<size_t>(part_base, 1) * sizeof(float4)));
+        NB_BCUDA(b, dev_alloc(&b->part, std::max<size_t>(part_base, 1) * sizeof(float4)));
         b->part_cap = part_base;
     }
     b->graph_dirty = true;
@@ -263,12 +263,12 @@ int reserve_tree(nb_batch* b, size_t n_int, size_t n_cells) {
     NB_BCUDA(b, tree_reserve_graph(b->core, (int)b->n_bh, n_int, n_cells));
     const size_t cap = b->core->tree.cell_cap;
     if (cap > b->qcap) {
-        cudaFree(b->cell_q1); cudaFree(b->cell_q2); cudaFree(b->cell_walk);
+        for (void* p : {(void*)b->cell_q1, (void*)b->cell_q2, (void*)b->cell_walk}) dev_free(p, b->core->stream);
         b->cell_q1 = b->cell_q2 = nullptr;
         b->cell_walk = nullptr;
-        NB_BCUDA(b, cudaMalloc(&b->cell_q1, cap * sizeof(float4)));
-        NB_BCUDA(b, cudaMalloc(&b->cell_q2, cap * sizeof(float4)));
-        NB_BCUDA(b, cudaMalloc(&b->cell_walk, cap * sizeof(int4)));
+        NB_BCUDA(b, dev_alloc(&b->cell_q1, cap * sizeof(float4)));
+        NB_BCUDA(b, dev_alloc(&b->cell_q2, cap * sizeof(float4)));
+        NB_BCUDA(b, dev_alloc(&b->cell_walk, cap * sizeof(int4)));
         b->qcap = cap;
     }
     b->graph_dirty = true;
@@ -462,7 +462,7 @@ int nb_batch_create(const nb_params* base, size_t bh_threshold, double bh_theta,
         b->bh_threshold = bh_threshold;
         b->bh_theta = bh_theta;
         b->core = core;
-        if (cudaMalloc(&b->next_unit, sizeof(int)) != cudaSuccess || cudaMalloc(&b->held, sizeof(int)) != cudaSuccess) {
+        if (dev_alloc(&b->next_unit, sizeof(int)) != cudaSuccess || dev_alloc(&b->held, sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
             nb_batch_destroy(b);
             return NB_ENOMEM;
@@ -483,7 +483,7 @@ int nb_batch_destroy(nb_batch* b) {
         void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
                         b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
                         b->unit_comp, b->part, b->next_unit, b->held};
-        for (void* p : ptrs) cudaFree(p);
+        for (void* p : ptrs) dev_free(p, b->core ? b->core->stream : nullptr);
         if (b->core) nb_destroy(b->core);
         delete b;
         return NB_OK;
@@ -632,18 +632,18 @@ int nb_batch_commit(nb_batch* b) {
                 NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
                                             b->core->stream));
         }
-        NB_BCUDA(b, upload(&b->body_slot, body_slot));
-        NB_BCUDA(b, upload(&b->slot_start, slot_start));
-        NB_BCUDA(b, upload(&b->gal_range, gal_range));
-        NB_BCUDA(b, upload(&b->body_dgal, body_dgal));
+        NB_BCUDA(b, upload(&b->body_slot, body_slot, b->core->stream));
+        NB_BCUDA(b, upload(&b->slot_start, slot_start, b->core->stream));
+        NB_BCUDA(b, upload(&b->gal_range, gal_range, b->core->stream));
+        NB_BCUDA(b, upload(&b->body_dgal, body_dgal, b->core->stream));
         if (b->nslot > 0) {
-            NB_BCUDA(b, cudaMalloc(&b->gal_box, b->nslot * sizeof(float4)));
-            NB_BCUDA(b, cudaMalloc(&b->gal_root, b->nslot * sizeof(int32_t)));
-            NB_BCUDA(b, cudaMalloc(&b->box_bits, 6 * b->nslot * sizeof(unsigned)));
+            NB_BCUDA(b, dev_alloc(&b->gal_box, b->nslot * sizeof(float4)));
+            NB_BCUDA(b, dev_alloc(&b->gal_root, b->nslot * sizeof(int32_t)));
+            NB_BCUDA(b, dev_alloc(&b->box_bits, 6 * b->nslot * sizeof(unsigned)));
             // groups are disjoint and non-empty: at most one per body
             b->group_cap = (int)b->n_bh;
-            NB_BCUDA(b, cudaMalloc(&b->groups, b->n_bh * sizeof(int4)));
-            NB_BCUDA(b, cudaMalloc(&b->group_ctr, 2 * sizeof(int)));
+            NB_BCUDA(b, dev_alloc(&b->groups, b->n_bh * sizeof(int4)));
+            NB_BCUDA(b, dev_alloc(&b->group_ctr, 2 * sizeof(int)));
         }
         b->h_pos.clear();
         b->h_vel.clear();
@@ -842,7 +842,7 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
         nb_sim* c = b->core;
         const size_t bytes = c->n_pad * sizeof(float4);
         float4* save = nullptr;
-        NB_BCUDA(b, cudaMalloc(&save, 5 * bytes));
+        NB_BCUDA(b, dev_alloc(&save, 5 * bytes));
         // the state and the accelerations the far field's relative rule reads
         auto snapshot = [&](bool restore) {
             float4* arrs[5] = {c->pos, c->posc, c->vel, c->velc, c->acc};
@@ -899,7 +899,7 @@ int nb_batch_autotune(nb_batch* b, float dt, int trial_steps) {
         cudaEventDestroy(e1);
         snapshot(true);
         cudaStreamSynchronize(c->stream);
-        cudaFree(save);
+        dev_free(save, c->stream);
         if (rc) return rc;
         return nb_batch_set_tuning(b, &best);
     } catch (...) {   // no exception crosses the C-ABI: host allocation failed

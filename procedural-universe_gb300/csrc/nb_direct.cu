@@ -323,10 +323,10 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     const int splits = direct_splits(sim, t, sim->n_pad);
     const size_t need = (size_t)splits * 2 * sim->n_pad;
     if (need > sim->part_cap) {
-        if (sim->part) cudaFree(sim->part);
+        dev_free(sim->part, sim->stream);
         sim->part = nullptr;
         sim->part_cap = 0;
-        cudaError_t e = cudaMalloc(&sim->part, need * sizeof(float4));
+        cudaError_t e = dev_alloc(&sim->part, need * sizeof(float4));
         if (e != cudaSuccess) return e;
         sim->part_cap = need;
     }

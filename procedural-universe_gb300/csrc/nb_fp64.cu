@@ -174,10 +174,10 @@ cudaError_t fp64_diagnostics_ex(nb_sim* sim, float half_dt, bool with_acc, bool 
     const int nblocks = (int)(sim->n_pad / kF64Block);
     const size_t need = (size_t)nblocks * kDiagTerms;
     if (need > sim->dscratch_cap) {
-        if (sim->dscratch) cudaFree(sim->dscratch);
+        dev_free(sim->dscratch, sim->stream);
         sim->dscratch = nullptr;
         sim->dscratch_cap = 0;
-        cudaError_t e = cudaMalloc(&sim->dscratch, need * sizeof(double));
+        cudaError_t e = dev_alloc(&sim->dscratch, need * sizeof(double));
         if (e != cudaSuccess) return e;
         sim->dscratch_cap = need;
     }

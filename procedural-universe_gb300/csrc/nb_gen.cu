@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_write(const GenGal* __restr
 
 template <typename T>
 cudaError_t upload_async(T** d, const std::vector<T>& h, cudaStream_t st) {
-    cudaError_t e = cudaMalloc(d, std::max<size_t>(1, h.size()) * sizeof(T));
+    cudaError_t e = dev_alloc(d, std::max<size_t>(1, h.size()) * sizeof(T));
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st);
 }
@@ -156,8 +156,8 @@ cudaError_t gen_galaxies(const std::vector<GenSpec>& specs, float4* pos, float4*
     cudaError_t e = upload_async(&d_gals, gals, st);
     if (e == cudaSuccess) e = upload_async(&d_chunks, chunks, st);
     if (e == cudaSuccess) e = upload_async(&d_gal_chunks, gal_chunks, st);
-    if (e == cudaSuccess) e = cudaMalloc(&d_part, 7 * chunks.size() * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&d_com, 6 * gals.size() * sizeof(double));
+    if (e == cudaSuccess) e = dev_alloc(&d_part, 7 * chunks.size() * sizeof(double));
+    if (e == cudaSuccess) e = dev_alloc(&d_com, 6 * gals.size() * sizeof(double));
     if (e == cudaSuccess) {
         k_gen_sums<<<(unsigned)chunks.size(), kGenThreads, 0, st>>>(d_gals, d_chunks, d_part);
         k_gen_centre<<<(unsigned)((gals.size() + 127) / 128), 128, 0, st>>>(d_gal_chunks, (int)gals.size(), d_part,
@@ -167,11 +167,7 @@ cudaError_t gen_galaxies(const std::vector<GenSpec>& specs, float4* pos, float4*
     }
     const cudaError_t es = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = es;
-    cudaFree(d_gals);
-    cudaFree(d_chunks);
-    cudaFree(d_gal_chunks);
-    cudaFree(d_part);
-    cudaFree(d_com);
+    for (void* p : {(void*)d_gals, (void*)d_chunks, (void*)d_gal_chunks, (void*)d_part, (void*)d_com}) dev_free(p, st);
     return e;
 }
 

@@ -283,6 +283,21 @@ class PhaseScope {
     cudaEvent_t b_ = nullptr;
 };
 
+// ---- device memory (nb_api.cu) ----
+// The library's device buffers come from one memory pool per device that
+// keeps freed memory for later allocations: a served batch rebuilt every few
+// rounds allocates and frees gigabytes, which cudaMalloc / cudaFree would map
+// and unmap each time (and every cudaFree waits for the whole device).
+// dev_alloc: the buffer may be used on any stream when it returns.
+// dev_free: returns the buffer after the work already queued on st (the
+// stream every use of the buffer was queued on).
+cudaError_t dev_alloc(void** p, size_t bytes);
+template <typename T>
+cudaError_t dev_alloc(T** p, size_t bytes) {
+    return dev_alloc(reinterpret_cast<void**>(p), bytes);
+}
+void dev_free(void* p, cudaStream_t st);
+
 // ---- misc ----
 cudaError_t render_fill(nb_sim* sim, const float4* d_colour, float scale, nb_render_vertex* d_out);
 

@@ -772,10 +772,12 @@ __global__ void __launch_bounds__(kSortThreads) k_batch_keys_hist(
 }
 
 // --------------------------------------------------------------- host ----
-static cudaError_t grow(void** p, size_t bytes) {
-    if (*p) cudaFree(*p);
+// Replaces *p by a buffer of `bytes` (the old one returned after the work
+// queued on st).
+static cudaError_t grow(void** p, size_t bytes, cudaStream_t st) {
+    dev_free(*p, st);
     *p = nullptr;
-    return cudaMalloc(p, bytes);
+    return dev_alloc(p, bytes);
 }
 
 #define NB_TRY(x)                               \
@@ -788,28 +790,28 @@ static cudaError_t reserve_bodies(nb_sim* sim, size_t nk) {
     TreeBuffers& t = sim->tree;
     if (nk <= t.body_cap) return cudaSuccess;
     const size_t cap = nk;
-    NB_TRY(grow((void**)&t.keys[0], cap * 8));
-    NB_TRY(grow((void**)&t.keys[1], cap * 8));
-    NB_TRY(grow((void**)&t.vals[0], cap * 4));
-    NB_TRY(grow((void**)&t.vals[1], cap * 4));
-    NB_TRY(grow((void**)&t.depth, cap * 4));
-    NB_TRY(grow((void**)&t.spos, cap * 16));
-    NB_TRY(grow((void**)&t.pos_nint, cap * 4));
-    NB_TRY(grow((void**)&t.leaf_level, cap * 4));
-    NB_TRY(grow((void**)&t.leaf_count, cap * 4));
-    NB_TRY(grow((void**)&t.leaf_parent, cap * 4));
+    NB_TRY(grow((void**)&t.keys[0], cap * 8, sim->stream));
+    NB_TRY(grow((void**)&t.keys[1], cap * 8, sim->stream));
+    NB_TRY(grow((void**)&t.vals[0], cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.vals[1], cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.depth, cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.spos, cap * 16, sim->stream));
+    NB_TRY(grow((void**)&t.pos_nint, cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.leaf_level, cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.leaf_count, cap * 4, sim->stream));
+    NB_TRY(grow((void**)&t.leaf_parent, cap * 4, sim->stream));
     const size_t ntiles = cap / kSortTile;
-    NB_TRY(grow((void**)&t.sort_status, (size_t)kPasses * ntiles * 256 * sizeof(unsigned long long)));
-    NB_TRY(grow((void**)&t.pos_status, ntiles * sizeof(unsigned long long)));
-    if (!t.plan) NB_TRY(cudaMalloc(&t.plan, 32 * 4));
-    if (!t.dig_off) NB_TRY(cudaMalloc(&t.dig_off, kPasses * 256 * 4));
+    NB_TRY(grow((void**)&t.sort_status, (size_t)kPasses * ntiles * 256 * sizeof(unsigned long long), sim->stream));
+    NB_TRY(grow((void**)&t.pos_status, ntiles * sizeof(unsigned long long), sim->stream));
+    if (!t.plan) NB_TRY(dev_alloc(&t.plan, 32 * 4));
+    if (!t.dig_off) NB_TRY(dev_alloc(&t.dig_off, kPasses * 256 * 4));
     if (!t.counters) {
         // counters, tile counters of the look-back kernels, then the radix histograms
-        NB_TRY(cudaMalloc(&t.counters, (kCounterWords + kPasses * 256) * 4));
+        NB_TRY(dev_alloc(&t.counters, (kCounterWords + kPasses * 256) * 4));
         t.ghist = reinterpret_cast<uint32_t*>(t.counters + kCounterWords);
     }
     if (!t.h_counters) NB_TRY(cudaMallocHost(&t.h_counters, TC_COUNT * 4));
-    if (!t.interactions) NB_TRY(cudaMalloc(&t.interactions, sizeof(unsigned long long)));
+    if (!t.interactions) NB_TRY(dev_alloc(&t.interactions, sizeof(unsigned long long)));
     t.body_cap = cap;
     return cudaSuccess;
 }
@@ -818,34 +820,34 @@ static cudaError_t reserve_nodes(nb_sim* sim, size_t n_int, size_t n_cells) {
     TreeBuffers& t = sim->tree;
     if (n_int > t.int_cap) {
         const size_t cap = n_int + n_int / 4 + 64;
-        NB_TRY(grow((void**)&t.int_level, cap * 4));
-        NB_TRY(grow((void**)&t.int_first, cap * 4));
-        NB_TRY(grow((void**)&t.int_parent, cap * 4));
-        NB_TRY(grow((void**)&t.int_mask, cap * 4));
-        NB_TRY(grow((void**)&t.int_nint, cap * 4));
-        NB_TRY(grow((void**)&t.int_pending, cap * 4));
-        NB_TRY(grow((void**)&t.int_block, cap * 4));
-        NB_TRY(grow((void**)&t.int_cell, cap * 4));
-        NB_TRY(grow((void**)&t.int_code, cap * 8));
+        NB_TRY(grow((void**)&t.int_level, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_first, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_parent, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_mask, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_nint, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_pending, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_block, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_cell, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.int_code, cap * 8, sim->stream));
         // internal nodes can outnumber bodies (chains of one-child nodes above
         // close pairs): the child-count scan's status is sized by them
-        NB_TRY(grow((void**)&t.popc_status, ((cap + kSortTile - 1) / kSortTile) * sizeof(unsigned long long)));
+        NB_TRY(grow((void**)&t.popc_status, ((cap + kSortTile - 1) / kSortTile) * sizeof(unsigned long long), sim->stream));
         t.int_cap = cap;
         size_t h = 1024;
         while (h < 2 * cap) h <<= 1;
-        NB_TRY(grow((void**)&t.hkeys, h * 8));
-        NB_TRY(grow((void**)&t.hvals, h * 4));
+        NB_TRY(grow((void**)&t.hkeys, h * 8, sim->stream));
+        NB_TRY(grow((void**)&t.hvals, h * 4, sim->stream));
         t.hash_cap = h;
     }
     if (n_cells > t.cell_cap) {
         const size_t cap = n_cells + n_cells / 4 + 64;
-        NB_TRY(grow((void**)&t.cell_com, cap * 16));
-        NB_TRY(grow((void**)&t.cell_meta, cap * 16));
-        NB_TRY(grow((void**)&t.cell_mass, cap * 8));
-        NB_TRY(grow((void**)&t.cell_count, cap * 4));
-        NB_TRY(grow((void**)&t.cell_lo, cap * 16));
-        NB_TRY(grow((void**)&t.cell_hi, cap * 16));
-        NB_TRY(grow((void**)&t.cell_code, cap * 8));
+        NB_TRY(grow((void**)&t.cell_com, cap * 16, sim->stream));
+        NB_TRY(grow((void**)&t.cell_meta, cap * 16, sim->stream));
+        NB_TRY(grow((void**)&t.cell_mass, cap * 8, sim->stream));
+        NB_TRY(grow((void**)&t.cell_count, cap * 4, sim->stream));
+        NB_TRY(grow((void**)&t.cell_lo, cap * 16, sim->stream));
+        NB_TRY(grow((void**)&t.cell_hi, cap * 16, sim->stream));
+        NB_TRY(grow((void**)&t.cell_code, cap * 8, sim->stream));
         t.cell_cap = cap;
     }
     return cudaSuccess;
@@ -862,7 +864,7 @@ void tree_free(nb_sim* sim) {
                     t.int_pending, t.int_block, t.int_cell, t.int_code, t.cell_com, t.cell_meta, t.cell_mass,
                     t.cell_lo, t.cell_hi, t.cell_code, t.cell_count, t.hkeys, t.hvals, t.sort_status, t.pos_status,
                     t.popc_status, t.dig_off, t.plan, t.counters, t.interactions};
-    for (void* p : ptrs) cudaFree(p);
+    for (void* p : ptrs) dev_free(p, sim->stream);
     if (t.h_counters) cudaFreeHost(t.h_counters);
     t = TreeBuffers{};
 }
