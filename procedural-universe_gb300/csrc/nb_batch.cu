@@ -575,8 +575,11 @@ int nb_batch_commit(nb_batch* b) {
         b->ndgal = dgi;
         b->n_total = off;
         if (b->n_total > (size_t)INT32_MAX / 2) return bfail(b, NB_EINVAL, "batch too large");
-        std::vector<int32_t> body_slot(b->n_bh), slot_start(b->nslot), body_dgal(b->n_total - b->dir_begin, -1);
-        std::vector<int4> gal_range(b->nslot);
+        // per-body galaxy tables, filled on the device from runs of at most
+        // kFillChunk bodies (begin, count, galaxy, table: 0 slot of a Barnes-Hut
+        // body, 1 direct-sum galaxy of a direct body, -1 on its padding)
+        std::vector<int32_t> slot_start(b->nslot);
+        std::vector<int4> gal_range(b->nslot), fill;
         b->n_real = 0;
         // state: zeroed arrays (padding bodies are zero-mass at the origin), host
         // galaxies copied in and validated
@@ -594,12 +597,12 @@ int nb_batch_commit(nb_batch* b) {
                                             b->core->stream));
             }
             b->n_real += g.n;
+            const size_t t0 = g.bh ? g.off : g.off - b->dir_begin;
+            for (size_t c = 0; c < g.n; c += kFillChunk)
+                fill.push_back(make_int4((int)(t0 + c), (int)std::min<size_t>(kFillChunk, g.n - c), g.idx, g.bh ? 0 : 1));
             if (g.bh) {
-                for (size_t i = 0; i < g.n; ++i) body_slot[g.off + i] = g.idx;
                 slot_start[g.idx] = (int)g.off;
                 gal_range[g.idx] = make_int4((int)g.off, (int)g.n, 0, 0);
-            } else {
-                for (size_t i = 0; i < g.n; ++i) body_dgal[g.off - b->dir_begin + i] = g.idx;
             }
         }
         // galaxies generated on the device, straight into the state arrays
@@ -632,10 +635,27 @@ int nb_batch_commit(nb_batch* b) {
                 NB_BCUDA(b, cudaMemcpyAsync(dst[a] + g.off, g.dsrc[a], g.n * sizeof(float4), cudaMemcpyDeviceToDevice,
                                             b->core->stream));
         }
-        NB_BCUDA(b, upload(&b->body_slot, body_slot, b->core->stream));
         NB_BCUDA(b, upload(&b->slot_start, slot_start, b->core->stream));
         NB_BCUDA(b, upload(&b->gal_range, gal_range, b->core->stream));
-        NB_BCUDA(b, upload(&b->body_dgal, body_dgal, b->core->stream));
+        {
+            cudaStream_t st = b->core->stream;
+            dev_free(b->body_slot, st);
+            dev_free(b->body_dgal, st);
+            b->body_slot = b->body_dgal = nullptr;
+            if (b->n_bh > 0) NB_BCUDA(b, dev_alloc(&b->body_slot, b->n_bh * sizeof(int32_t)));
+            const size_t nd = b->n_total - b->dir_begin;
+            if (nd > 0) {
+                NB_BCUDA(b, dev_alloc(&b->body_dgal, nd * sizeof(int32_t)));
+                NB_BCUDA(b, cudaMemsetAsync(b->body_dgal, 0xff, nd * sizeof(int32_t), st));   // padding: -1
+            }
+            int4* d_fill = nullptr;
+            NB_BCUDA(b, upload(&d_fill, fill, st));
+            if (!fill.empty())
+                k_fill_tables<<<(unsigned)fill.size(), 256, 0, st>>>(d_fill, b->body_slot, b->body_dgal);
+            const cudaError_t e = cudaGetLastError();
+            dev_free(d_fill, st);
+            NB_BCUDA(b, e);
+        }
         if (b->nslot > 0) {
             NB_BCUDA(b, dev_alloc(&b->gal_box, b->nslot * sizeof(float4)));
             NB_BCUDA(b, dev_alloc(&b->gal_root, b->nslot * sizeof(int32_t)));

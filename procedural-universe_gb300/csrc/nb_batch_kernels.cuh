@@ -50,6 +50,16 @@ constexpr double kFarCap = 0.5;         // relative rule: largest half-diagonal 
 
 enum : int { BK_SINGLE = 1, BK_BUCKET = 2, BK_INTERNAL = 3 };
 
+// ---- per-body galaxy tables -------------------------------------------------
+constexpr int kFillChunk = 8192;   // bodies per block of the table fill
+// run = (first entry, entries, value, table): table 0 is the Barnes-Hut bodies'
+// slot, table 1 the direct-sum bodies' galaxy.
+__global__ void k_fill_tables(const int4* __restrict__ runs, int32_t* __restrict__ slot, int32_t* __restrict__ dgal) {
+    const int4 r = runs[blockIdx.x];
+    int32_t* out = r.w ? dgal : slot;
+    for (int i = threadIdx.x; i < r.y; i += blockDim.x) out[r.x + i] = r.z;
+}
+
 // ---- bounding cube of each Barnes-Hut galaxy ------------------------------
 // Min/max are exact and order-free, so chunks of kBoxChunk bodies reduce in
 // parallel into per-galaxy words with atomics on an order-preserving integer
