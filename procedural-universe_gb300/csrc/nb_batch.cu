@@ -60,9 +60,7 @@ struct nb_batch {
     int group_cap = 0;
     int* group_ctr = nullptr;        // [0] groups emitted, [1] next group to traverse
     unsigned* box_bits = nullptr;    // 6 ordered words per galaxy: min xyz, max xyz
-    float4* cell_q1 = nullptr;
-    float4* cell_q2 = nullptr;
-    int4* cell_walk = nullptr;      // per cell: (first child | first body, count, first body, kind | children << 4 | level << 8)
+    CellRec* cell_rec = nullptr;    // per cell: centre of mass, walk record, quadrupole (nb_cellrec.cuh)
     size_t qcap = 0;
     // direct-sum tables
     int32_t* body_dgal = nullptr;
@@ -192,19 +190,18 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
                                                                                        b->nslot, b->box_bits);
         }
         NB_BCUDA(b, tree_batch_keys(c, c->pos, b->body_slot, n, b->box_bits, b->nslot, b->gal_box));
-        NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth, tree_only));
+        NB_BCUDA(b, tree_build_graph(c, c->pos, n, kBatchDepth, tree_only, b->cell_rec));
         if (tree_only) return NB_OK;
         {
             PhaseScope ps(c, NB_PHASE_MASS, 3);
             k_batch_moments<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
                 (int)t.int_cap, t.counters, t.int_parent, t.int_nint, t.int_pending, t.int_cell, t.int_block,
-                t.int_mask, t.int_first, t.spos, t.cell_com, b->cell_q1, b->cell_q2, t.cell_count, b->cell_walk,
-                t.cell_meta, t.cell_hi, (int)t.cell_cap, n, c->d_err);
+                t.int_mask, t.int_first, t.int_level, b->cell_rec, (int)t.cell_cap, c->d_err);
             k_batch_roots<<<(b->nslot + 127) / 128, 128, 0, st>>>(b->slot_start, b->nslot, t.keys[0], t.pos_nint,
                                                                  t.int_cell, t.counters, (int)t.int_cap,
                                                                  (int)t.cell_cap, b->gal_root, c->d_err);
             k_batch_groups<<<(unsigned)((t.int_cap + 255) / 256), 256, 0, st>>>(
-                (int)t.int_cap, t.counters, t.int_cell, b->cell_walk,
+                (int)t.int_cap, t.counters, t.int_cell, b->cell_rec,
                 t.vals[0], b->body_slot, (int)t.cell_cap, n, b->groups, b->group_cap, b->group_ctr, c->d_err);
         }
         {
@@ -220,8 +217,8 @@ int enqueue_step(nb_batch* b, float dt, bool update, bool tree_only = false) {
             const int blocks = std::max(1, std::min(max_blocks, c->sm_count * std::max(1, occ)));
 #define NB_GT(L)                                                                                                  \
     k_group_traverse<L><<<blocks, kGWarps * 32, 0, st>>>(                                                         \
-        b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], t.cell_com, b->cell_walk,     \
-        b->cell_q1, b->cell_q2, b->gal_box, b->gal_root, b->nslot,                                                \
+        b->groups, b->group_ctr, b->group_cap, b->group_ctr + 1, t.spos, t.vals[0], b->cell_rec, b->gal_box,      \
+        b->gal_root, b->nslot,                                                                                    \
         (int)t.cell_cap, n, (int)t.int_cap, b->tune.leaf_size, th * th, S, G, (float)(b->far_eta * b->far_eta),   \
         (float)(b->far_alpha / b->base.G), (float)(b->far_cap * b->far_cap),                                      \
         100.f * S, c->d_mmax, c->acc, t.interactions, c->d_err)
@@ -263,12 +260,9 @@ int reserve_tree(nb_batch* b, size_t n_int, size_t n_cells) {
     NB_BCUDA(b, tree_reserve_graph(b->core, (int)b->n_bh, n_int, n_cells));
     const size_t cap = b->core->tree.cell_cap;
     if (cap > b->qcap) {
-        for (void* p : {(void*)b->cell_q1, (void*)b->cell_q2, (void*)b->cell_walk}) dev_free(p, b->core->stream);
-        b->cell_q1 = b->cell_q2 = nullptr;
-        b->cell_walk = nullptr;
-        NB_BCUDA(b, dev_alloc(&b->cell_q1, cap * sizeof(float4)));
-        NB_BCUDA(b, dev_alloc(&b->cell_q2, cap * sizeof(float4)));
-        NB_BCUDA(b, dev_alloc(&b->cell_walk, cap * sizeof(int4)));
+        dev_free(b->cell_rec, b->core->stream);
+        b->cell_rec = nullptr;
+        NB_BCUDA(b, dev_alloc(&b->cell_rec, cap * sizeof(CellRec)));
         b->qcap = cap;
     }
     b->graph_dirty = true;
@@ -481,7 +475,7 @@ int nb_batch_destroy(nb_batch* b) {
         if (b->core && b->core->stream) cudaStreamSynchronize(b->core->stream);
         if (b->exec) cudaGraphExecDestroy(b->exec);
         void* ptrs[] = {b->body_slot, b->gal_range, b->gal_box, b->gal_root, b->slot_start, b->groups, b->group_ctr,
-                        b->box_bits, b->cell_q1, b->cell_q2, b->cell_walk, b->body_dgal, b->dgal, b->units,
+                        b->box_bits, b->cell_rec, b->body_dgal, b->dgal, b->units,
                         b->unit_comp, b->part, b->next_unit, b->held};
         for (void* p : ptrs) dev_free(p, b->core ? b->core->stream : nullptr);
         if (b->core) nb_destroy(b->core);

@@ -7,7 +7,8 @@
 //    levels), so ONE radix sort and ONE topology build make a forest whose
 //    level-7 nodes are the galaxy roots.
 //  * The mass pass adds traceless quadrupole moments (parallel-axis rule
-//    bottom-up) and a 16-byte walk record per cell.  Traversal groups are
+//    bottom-up); a cell's centre of mass, walk record and quadrupole form one
+//    64-byte record (nb_cellrec.cuh).  Traversal groups are
 //    taken from the tree itself: the largest subtrees of at most kGroupMax
 //    bodies whose cell is at most 1/16 of the galaxy cube, consecutive small
 //    siblings packed together, oversized depth-cap buckets cut into chunks --
@@ -30,6 +31,7 @@
 #include <type_traits>
 
 #include "nb_morton.cuh"
+#include "nb_cellrec.cuh"
 
 namespace nb {
 
@@ -48,7 +50,6 @@ constexpr double kFarEta = 0.2;         // geometric rule: group half-diagonal /
 constexpr double kFarAlpha = 1e-4;      // relative rule: truncation estimate / (|a|_min / G)
 constexpr double kFarCap = 0.5;         // relative rule: largest half-diagonal / distance
 
-enum : int { BK_SINGLE = 1, BK_BUCKET = 2, BK_INTERNAL = 3 };
 
 // ---- per-body galaxy tables -------------------------------------------------
 constexpr int kFillChunk = 8192;   // bodies per block of the table fill
@@ -128,38 +129,11 @@ __global__ void __launch_bounds__(256) k_gal_box_chunks(const float4* __restrict
 // ---- bottom-up mass, centre of mass and quadrupole --------------------------
 // Q_ij = sum m (3 y_i y_j - |y|^2 d_ij), y = offset from the node's centre of
 // mass; a parent sums its children's Q plus m_c (3 d d - |d|^2 I), d = com_c - com.
-__device__ void bucket_moments(const float4* spos, int first, int count, float4& cm, float4& q1, float4& q2) {
-    float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    for (int q = first; q < first + count; ++q) {
-        const float4 b = spos[q];
-        m += b.w; cx = fmaf(b.w, b.x, cx); cy = fmaf(b.w, b.y, cy); cz = fmaf(b.w, b.z, cz);
-    }
-    const float im = m > 0.f ? 1.f / m : 0.f;
-    cx *= im; cy *= im; cz *= im;
-    float xx = 0.f, yy = 0.f, zz = 0.f, xy = 0.f, xz = 0.f, yz = 0.f;
-    for (int q = first; q < first + count; ++q) {
-        const float4 b = spos[q];
-        const float dx = b.x - cx, dy = b.y - cy, dz = b.z - cz, r2 = dx * dx + dy * dy + dz * dz;
-        xx += b.w * (3.f * dx * dx - r2); yy += b.w * (3.f * dy * dy - r2); zz += b.w * (3.f * dz * dz - r2);
-        xy += b.w * 3.f * dx * dy; xz += b.w * 3.f * dx * dz; yz += b.w * 3.f * dy * dz;
-    }
-    cm = make_float4(cx, cy, cz, m);
-    q1 = make_float4(xx, yy, zz, 0.f);
-    q2 = make_float4(xy, xz, yz, 0.f);
-}
-
-// A cell's walk record packs what the traversal reads of it besides its centre
-// of mass: (first child or, for a leaf, first body; bodies; first body;
-// kind | children << 4 | level << 8).  A node writes its own and its leaf
-// children's.
-__device__ __forceinline__ int4 walk_record(int F, int count, int first, int kind, int nch, int level) {
-    return make_int4(F, count, first, kind | (nch << 4) | (level << 8));
-}
-
+// Leaf records are written by the placement (nb_cellrec.cuh); an internal
+// node reads its children's records (contiguous) and writes its own whole.
 __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* int_block, const uint32_t* int_mask,
-                               const int32_t* int_first, const float4* spos, float4* cell_com, float4* cell_q1,
-                               float4* cell_q2, int32_t* cell_count, int4* cell_walk, const int4* cell_meta,
-                               const float4* cell_hi, int cell_cap, int nbodies, int* err) {
+                               const int32_t* int_first, const int32_t* int_level, CellRec* rec, int cell_cap,
+                               int* err) {
     const int c = int_cell[k];
     const int F = 1 + int_block[k];
     const int nch = __popc(int_mask[k]);
@@ -167,36 +141,17 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
         record_error(err, DEV_TREE_OVERFLOW);
         return;
     }
-    // children sit one level below their node (a node exists at every level
-    // where two or more bodies still share the key prefix)
-    const int level = (int)__ldcg(&cell_hi[c]).w;
     float4 ccm[8], cq1[8], cq2[8];
     float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     int count = 0;
     for (int j = 0; j < nch; ++j) {
-        const int ch = F + j;
-        const int4 mt = __ldcg(&cell_meta[ch]);
-        const int kind = mt.w & 15;
-        const int cnt = __ldcg(&cell_count[ch]);
-        if (kind == BK_INTERNAL) {
-            ccm[j] = __ldcg(&cell_com[ch]);
-            cq1[j] = __ldcg(&cell_q1[ch]);
-            cq2[j] = __ldcg(&cell_q2[ch]);
-        } else if (kind == BK_BUCKET) {
-            if (mt.x < 0 || cnt < 0 || mt.x + cnt > nbodies) {
-                record_error(err, DEV_TREE_OVERFLOW);
-                ccm[j] = cq1[j] = cq2[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-                continue;
-            }
-            bucket_moments(spos, mt.x, cnt, ccm[j], cq1[j], cq2[j]);
-        } else {
-            ccm[j] = __ldcg(&cell_com[ch]);
-            cq1[j] = cq2[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        if (kind != BK_INTERNAL) __stcg(&cell_walk[ch], walk_record(mt.x, cnt, mt.x, kind, 0, level + 1));
+        const CellRec* r = rec + F + j;
+        ccm[j] = __ldcg(&r->com);
+        count += __ldcg(&r->walk).y;
+        cq1[j] = __ldcg(&r->q1);
+        cq2[j] = __ldcg(&r->q2);
         m += ccm[j].w;
         cx = fmaf(ccm[j].w, ccm[j].x, cx); cy = fmaf(ccm[j].w, ccm[j].y, cy); cz = fmaf(ccm[j].w, ccm[j].z, cz);
-        count += cnt;
     }
     const float im = m > 0.f ? 1.f / m : 0.f;
     cx *= im; cy *= im; cz *= im;
@@ -211,30 +166,27 @@ __device__ void finish_moments(int k, const int32_t* int_cell, const int32_t* in
         xz += cq2[j].y + mc * 3.f * dx * dz;
         yz += cq2[j].z + mc * 3.f * dy * dz;
     }
-    __stcg(&cell_com[c], make_float4(cx, cy, cz, m));
-    __stcg(&cell_q1[c], make_float4(xx, yy, zz, 0.f));
-    __stcg(&cell_q2[c], make_float4(xy, xz, yz, 0.f));
-    __stcg(&cell_count[c], count);
-    __stcg(&cell_walk[c], walk_record(F, count, int_first[k], BK_INTERNAL, nch, level));
+    CellRec* r = rec + c;
+    __stcg(&r->com, make_float4(cx, cy, cz, m));
+    __stcg(&r->walk, walk_record(F, count, int_first[k], BK_INTERNAL, nch, int_level[k]));
+    __stcg(&r->q1, make_float4(xx, yy, zz, 0.f));
+    __stcg(&r->q2, make_float4(xy, xz, yz, 0.f));
 }
 
+// One thread per internal node whose children are all leaves; the last child
+// of a node to finish finishes the node (acquire-release counter per node).
 __global__ void k_batch_moments(int int_cap, const int32_t* __restrict__ counters,
                                 const int32_t* __restrict__ int_parent, const int32_t* __restrict__ int_nint,
                                 int32_t* __restrict__ int_pending, const int32_t* __restrict__ int_cell,
                                 const int32_t* __restrict__ int_block, const uint32_t* __restrict__ int_mask,
-                                const int32_t* __restrict__ int_first, const float4* __restrict__ spos,
-                                float4* __restrict__ cell_com, float4* __restrict__ cell_q1,
-                                float4* __restrict__ cell_q2, int32_t* __restrict__ cell_count,
-                                int4* __restrict__ cell_walk, const int4* __restrict__ cell_meta,
-                                const float4* __restrict__ cell_hi, int cell_cap, int nbodies,
-                                int* __restrict__ err) {
+                                const int32_t* __restrict__ int_first, const int32_t* __restrict__ int_level,
+                                CellRec* __restrict__ rec, int cell_cap, int* __restrict__ err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (!tree_fits(counters, int_cap, cell_cap)) return;   // held step: no moments
     const int ni = min(counters[TC_NINT], int_cap);
     if (k >= ni || int_nint[k] != 0) return;
     for (int guard = 0; guard < 64; ++guard) {
-        finish_moments(k, int_cell, int_block, int_mask, int_first, spos, cell_com, cell_q1, cell_q2, cell_count,
-                       cell_walk, cell_meta, cell_hi, cell_cap, nbodies, err);
+        finish_moments(k, int_cell, int_block, int_mask, int_first, int_level, rec, cell_cap, err);
         if (k == 0) return;
         const int p = int_parent[k];
         if (p < 0 || p >= ni) return;
@@ -302,7 +254,7 @@ __device__ __forceinline__ bool groupable(int level, int count) {
 }
 
 __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ counters, const int32_t* __restrict__ int_cell,
-                               const int4* __restrict__ cell_walk, const int32_t* __restrict__ sorder,
+                               const CellRec* __restrict__ rec, const int32_t* __restrict__ sorder,
                                const int32_t* __restrict__ body_slot, int n_cells, int nbodies,
                                int4* __restrict__ groups, int cap, int* __restrict__ n_groups, int* __restrict__ err) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,7 +266,7 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ counters
         record_error(err, DEV_TREE_OVERFLOW);
         return;
     }
-    const int4 wr = cell_walk[c];
+    const int4 wr = rec[c].walk;
     const int level = wr.w >> 8;
     const int cnt = wr.y;
     if (level < kSlotLevels) return;
@@ -329,7 +281,7 @@ __global__ void k_batch_groups(int int_cap, const int32_t* __restrict__ counters
     int run_first = -1, run_cnt = 0;
     for (int j = 0; j < nch; ++j) {
         const int ch = F + j;
-        const int4 cw = cell_walk[ch];
+        const int4 cw = rec[ch].walk;
         const int kind = cw.w & 15;
         const int cc = cw.y;
         const int cf = cw.z;
@@ -532,8 +484,7 @@ __device__ __forceinline__ void far_eval(const FarField& f, float x, float y, fl
 template <int LAW>
 __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     const int4* __restrict__ groups, const int* __restrict__ n_groups_dev, int group_cap, int* __restrict__ next_group,
-    const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const float4* __restrict__ cell_com,
-    const int4* __restrict__ cell_walk, const float4* __restrict__ cell_q1, const float4* __restrict__ cell_q2,
+    const float4* __restrict__ spos, const int32_t* __restrict__ sorder, const CellRec* __restrict__ rec,
     const float4* __restrict__ gal_box, const int32_t* __restrict__ gal_root, int nslot, int n_cells, int nbodies,
     int max_pops, int leaf_size, float theta2, float S, float G, float far2, float far_rel, float far_cap2,
     float far_min_r2,
@@ -716,7 +667,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
     if (root < 1 || root >= n_cells) {
         bad = true;
     } else {
-        const int4 rw = __ldg(&cell_walk[root]);
+        const int4 rw = __ldg(&rec[root].walk);
         const int rF = rw.x, rn = (rw.w >> 4) & 15;
         if ((rw.w & 15) != BK_INTERNAL || rF < 1 || rn < 1 || rn > 8 || rF + rn > n_cells || rF >= kStackCellLimit) {
             bad = true;
@@ -761,8 +712,8 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
         int first = 0, count = 0, ch = 0, cF = 0, cn = 0;
         if (lane < T) {
             ch = qF + (lane - qx);
-            ccm = __ldg(&cell_com[ch]);
-            const int4 wr = __ldg(&cell_walk[ch]);
+            ccm = __ldg(&rec[ch].com);
+            const int4 wr = __ldg(&rec[ch].walk);
             const int kind = wr.w & 15;
             count = wr.y;
             first = wr.z;
@@ -793,7 +744,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
                     far = rg2 < far2 * r2X;
                 }
                 if (far && r2X > far_min_r2) {   // far: into the group's local expansion
-                    far_add<LAW>(&ffs[w][0][lane], 32, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]), Xx, Xy, Xz, S);
+                    far_add<LAW>(&ffs[w][0][lane], 32, ccm, __ldg(&rec[ch].q1), __ldg(&rec[ch].q2), Xx, Xy, Xz, S);
                     cnt += (unsigned)grp.z;
                     a_cell = false;   // accepted, not listed
                 }
@@ -809,7 +760,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 5) k_group_traverse(
             if (ncl + __popc(bc) > kGCells) flush_cells();
             if (a_cell) {
                 const int idx = ncl + __popc(bc & lt);
-                put_cell(lcl[w], idx, ccm, __ldg(&cell_q1[ch]), __ldg(&cell_q2[ch]));
+                put_cell(lcl[w], idx, ccm, __ldg(&rec[ch].q1), __ldg(&rec[ch].q2));
             }
             ncl += __popc(bc);
         }

@@ -220,8 +220,12 @@ cudaError_t tree_sizes(nb_sim* sim, int32_t* cells, int32_t* internal);
 float theta_float(double theta);   // smallest float >= theta
 // Batched form: topology of pre-computed keys without host synchronisation.
 // counts_only: stop once the node counts are known (no node is written, so
-// the node arrays may still be too small for the tree).
-cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only = false);
+// the node arrays may still be too small for the tree).  rec: the batched
+// form's cell records; its leaves are placed there (nb_cellrec.cuh) instead of
+// the plain path's per-cell arrays, and internal nodes get only their cell.
+struct CellRec;
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only = false,
+                             CellRec* rec = nullptr);
 // Words of the counters buffer (counters, tile counters, radix histograms)
 // that a batched step clears before its keys.
 int tree_counter_words();

@@ -40,6 +40,7 @@
 #include "nb_scan.cuh"
 #include "nb_lookback.cuh"
 #include "nb_morton.cuh"
+#include "nb_cellrec.cuh"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -587,7 +588,8 @@ __device__ __forceinline__ void place_internal(int k, const int32_t* __restrict_
                                                const int32_t* __restrict__ int_block, int ni, int cell_cap,
                                                float half, float theta_f, int32_t* __restrict__ int_cell,
                                                int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
-                                               float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
+                                               float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code,
+                                               bool batch) {
     if (k >= ni) return;
     const uint64_t code = int_code[k];
     const int l = int_level[k];
@@ -597,6 +599,7 @@ __device__ __forceinline__ void place_internal(int k, const int32_t* __restrict_
         return;
     }
     int_cell[k] = cell;
+    if (batch) return;   // the batched form's moment pass writes the node's record
     float3 lo, hi;
     float side;
     node_bounds(code, l, half, lo, hi, side);
@@ -617,7 +620,8 @@ __device__ __forceinline__ void place_leaf(int s, const TopoView& tv, const int3
                                            float half, float theta_f, float4* __restrict__ cell_com,
                                            double* __restrict__ cell_mass, int32_t* __restrict__ cell_count,
                                            int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
-                                           float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
+                                           float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code,
+                                           CellRec* __restrict__ rec) {
     if (s >= tv.n_in) return;
     const int lf = leaf_level[s];
     if (lf < 0) return;
@@ -625,6 +629,10 @@ __device__ __forceinline__ void place_leaf(int s, const TopoView& tv, const int3
     if (lf > 0 && (leaf_parent[s] < 0 || leaf_parent[s] >= tv.int_cap)) return;   // parent lost to an overflow
     const int cell = (lf == 0) ? 0 : child_cell(int_block, int_mask, leaf_parent[s], (int)(code & 7ull));
     if (cell >= tv.cell_cap) return;
+    if (rec) {   // the batched form: the leaf's whole record (bodies clamped to the sorted range)
+        write_leaf_record(rec + cell, spos, s, max(1, min(leaf_count[s], tv.n_in - s)), lf);
+        return;
+    }
     float3 lo, hi;
     float side;
     node_bounds(code, lf, half, lo, hi, side);
@@ -667,7 +675,9 @@ __device__ __forceinline__ void place_leaf(int s, const TopoView& tv, const int3
 
 // Every cell: blocks [0, int_blocks) place internal nodes (bounds, opening
 // thresholds, first child), the rest the leaf starting at each position
-// (bounds, thresholds, mass and centre of mass of its body or bucket).
+// (bounds, thresholds, mass and centre of mass of its body or bucket).  With
+// rec (the batched form) an internal node only gets its cell and a leaf its
+// 64-byte record.
 __global__ void k_place(const int32_t* __restrict__ int_level, const uint64_t* __restrict__ int_code,
                         const int32_t* __restrict__ int_parent, const uint32_t* __restrict__ int_mask,
                         const int32_t* __restrict__ int_block, int n_int, const int32_t* __restrict__ n_int_dev,
@@ -676,16 +686,16 @@ __global__ void k_place(const int32_t* __restrict__ int_level, const uint64_t* _
                         const float4* __restrict__ spos, float half, float theta_f, int32_t* __restrict__ int_cell,
                         float4* __restrict__ cell_com, double* __restrict__ cell_mass,
                         int32_t* __restrict__ cell_count, int4* __restrict__ cell_meta, float4* __restrict__ cell_lo,
-                        float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code) {
+                        float4* __restrict__ cell_hi, uint64_t* __restrict__ cell_code, CellRec* __restrict__ rec) {
     if ((int)blockIdx.x < int_blocks) {
         const int k = blockIdx.x * blockDim.x + threadIdx.x;
         const int ni = n_int_dev ? min(*n_int_dev, n_int) : n_int;
         place_internal(k, int_level, int_code, int_parent, int_mask, int_block, ni, tv.cell_cap, half, theta_f,
-                       int_cell, cell_meta, cell_lo, cell_hi, cell_code);
+                       int_cell, cell_meta, cell_lo, cell_hi, cell_code, rec != nullptr);
     } else {
         const int s = (blockIdx.x - int_blocks) * blockDim.x + threadIdx.x;
         place_leaf(s, tv, leaf_level, leaf_count, leaf_parent, int_mask, int_block, spos, half, theta_f, cell_com,
-                   cell_mass, cell_count, cell_meta, cell_lo, cell_hi, cell_code);
+                   cell_mass, cell_count, cell_meta, cell_lo, cell_hi, cell_code, rec);
     }
 }
 
@@ -967,7 +977,8 @@ cudaError_t tree_build(nb_sim* sim) {
         k_place<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask, t.int_block, ni,
                                                 nullptr, ib, tv, t.leaf_level, t.leaf_count, t.leaf_parent, t.spos,
                                                 sim->prm.bounds_half, tf, t.int_cell, t.cell_com, t.cell_mass,
-                                                t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+                                                t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code,
+                                                nullptr);
         NB_TRY(cudaGetLastError());
     }
     {
@@ -1026,7 +1037,7 @@ cudaError_t tree_batch_keys(nb_sim* sim, const float4* pos, const int32_t* body_
     return cudaGetLastError();
 }
 
-cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only) {
+cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool counts_only, CellRec* rec) {
     TreeBuffers& t = sim->tree;
     const size_t nk = pad_up(std::max<size_t>((size_t)n, 1), kSortTile);
     const int ntiles = (int)(nk / kSortTile);
@@ -1066,7 +1077,7 @@ cudaError_t tree_build_graph(nb_sim* sim, const float4* pos, int n, int D, bool 
     k_place<<<ib + nbk, kEmitBlock, 0, st>>>(t.int_level, t.int_code, t.int_parent, t.int_mask, t.int_block, icap,
                                             t.counters + TC_NINT, ib, tv, t.leaf_level, t.leaf_count, t.leaf_parent,
                                             t.spos, sim->prm.bounds_half, 1.0f, t.int_cell, t.cell_com, t.cell_mass,
-                                            t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code);
+                                            t.cell_count, t.cell_meta, t.cell_lo, t.cell_hi, t.cell_code, rec);
     return cudaGetLastError();
 }
 
