@@ -114,14 +114,54 @@ __device__ __forceinline__ void zero_tile_status(unsigned long long* sort_status
     if (threadIdx.x == 0) pos_status[blockIdx.x] = 0ull;
 }
 
+// Radix passes that the top bits make redundant.  Keys are grouped by their
+// top 4 bits (the root octant, and ~0 for bodies outside the root or tile
+// padding), which the top pass sorts.  A lower pass whose digit is the same
+// for every key of each group changes nothing in the final order: the top pass
+// orders the groups, and within a group that digit is constant, so the order
+// within the group is that of the passes below it.  Such a pass is skipped.
+// For a galaxy at the centre of the reference's +-4000 cube, the bits of
+// levels 2-7 are fixed within each root octant: two of the eight passes go.
+// The group bits are recorded as two ORs per group, of the keys and of their
+// complements (both start at zero with the counters): a bit varies within
+// group g where both have it.
+constexpr int kKeyGroups = 16;
+__device__ __forceinline__ unsigned long long* group_bits(uint32_t* ghist) {
+    return reinterpret_cast<unsigned long long*>(ghist + kPasses * 256);
+}
+
+// Adds a key to its group's bits in shared memory: one atomic pair per warp
+// when the warp's keys share a group (the common case once keys are in
+// galaxy or octant order), else one per lane.
+__device__ __forceinline__ void note_group(uint64_t key, unsigned long long* sh) {
+    const uint32_t g = (uint32_t)(key >> 60);
+    const uint32_t g0 = __shfl_sync(0xffffffffu, g, 0);
+    if (__all_sync(0xffffffffu, g == g0)) {
+        const uint32_t lo = (uint32_t)key, hi = (uint32_t)(key >> 32);
+        const unsigned long long o =
+            ((unsigned long long)__reduce_or_sync(0xffffffffu, hi) << 32) | __reduce_or_sync(0xffffffffu, lo);
+        const unsigned long long z =
+            ((unsigned long long)__reduce_or_sync(0xffffffffu, ~hi) << 32) | __reduce_or_sync(0xffffffffu, ~lo);
+        if ((threadIdx.x & 31) == 0) {
+            atomicOr(&sh[g0], o);
+            atomicOr(&sh[kKeyGroups + g0], z);
+        }
+    } else {
+        atomicOr(&sh[g], (unsigned long long)key);
+        atomicOr(&sh[kKeyGroups + g], (unsigned long long)~key);
+    }
+}
+
 // Adds a tile's digit histograms of every pass into ghist (bins that are
-// zero in this tile cost nothing).
-__device__ __forceinline__ void flush_hist(uint32_t (*h)[256], uint32_t* ghist) {
+// zero in this tile cost nothing), and its group bits after them.
+__device__ __forceinline__ void flush_hist(uint32_t (*h)[256], const unsigned long long* sh_groups, uint32_t* ghist) {
     __syncthreads();
     for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) {
         const uint32_t v = (&h[0][0])[i];
         if (v) atomicAdd(&ghist[i], v);
     }
+    if (threadIdx.x < 2 * kKeyGroups && sh_groups[threadIdx.x])
+        atomicOr(&group_bits(ghist)[threadIdx.x], sh_groups[threadIdx.x]);
 }
 
 // K2 + the radix sort's global histograms: one block per tile of kSortTile
@@ -133,7 +173,9 @@ __global__ void __launch_bounds__(kSortThreads) k_keys_hist(const float4* __rest
                                                             unsigned long long* __restrict__ sort_status, int ntiles,
                                                             unsigned long long* __restrict__ pos_status) {
     __shared__ uint32_t h[kPasses][256];
+    __shared__ unsigned long long sh_groups[2 * kKeyGroups];
     for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    if (threadIdx.x < 2 * kKeyGroups) sh_groups[threadIdx.x] = 0ull;
     zero_tile_status(sort_status, ntiles, pos_status);
     __syncthreads();
     for (int it = 0; it < kSortItems; ++it) {
@@ -149,6 +191,7 @@ __global__ void __launch_bounds__(kSortThreads) k_keys_hist(const float4* __rest
         keys[i] = key;
 #pragma unroll
         for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(key >> (8 * p)) & 255], 1u);
+        note_group(key, sh_groups);
         const uint32_t in_b = __ballot_sync(0xffffffffu, inside);
         const uint32_t gap_b = __ballot_sync(0xffffffffu, gap);
         if ((threadIdx.x & 31) == 0) {
@@ -156,21 +199,31 @@ __global__ void __launch_bounds__(kSortThreads) k_keys_hist(const float4* __rest
             if (gap_b) atomicAdd(&counters[TC_GAPS], __popc(gap_b));
         }
     }
-    flush_hist(h, ghist);
+    flush_hist(h, sh_groups, ghist);
 }
 
 // ------------------------------------------------------------ K3 radix sort --
-// plan[p] = 1 when every key has the same digit in pass p; plan[8+p] = buffer
-// the pass reads; plan[16] = buffer holding the result.  dig_off[p][d] = keys
+// plan[p] = 1 when pass p is skipped: every key has the same digit, or (below
+// the top pass) every key of each top group has (note_group); plan[8+p] =
+// buffer the pass reads; plan[16] = buffer holding the result.  dig_off[p][d] = keys
 // with a smaller digit than d in pass p (where digit d's keys start).
 __global__ void k_sort_plan(const uint32_t* __restrict__ ghist, int nk, int32_t* __restrict__ plan,
                             int32_t* __restrict__ dig_off) {
     __shared__ int triv[kPasses];
     __shared__ int sh_warp[33];
+    // bits that vary within some top group
+    __shared__ unsigned long long sh_var;
+    if (threadIdx.x == 0) {
+        const unsigned long long* gb = group_bits(const_cast<uint32_t*>(ghist));
+        unsigned long long var = 0ull;
+        for (int g = 0; g < kKeyGroups; ++g) var |= gb[g] & gb[kKeyGroups + g];
+        sh_var = var;
+    }
+    __syncthreads();
     for (int p = 0; p < kPasses; ++p) {
         const int c = (int)ghist[p * 256 + threadIdx.x];
         const int t = __syncthreads_or(c == nk);
-        if (threadIdx.x == 0) triv[p] = t;
+        if (threadIdx.x == 0) triv[p] = t || (p < kPasses - 1 && ((sh_var >> (8 * p)) & 255ull) == 0ull);
         int total;
         dig_off[p * 256 + threadIdx.x] = block_excl_scan(c, sh_warp, &total);
     }
@@ -759,10 +812,12 @@ __global__ void __launch_bounds__(kSortThreads) k_batch_keys_hist(
     int32_t* __restrict__ depth, uint32_t* __restrict__ ghist, unsigned long long* __restrict__ sort_status,
     int ntiles, unsigned long long* __restrict__ pos_status) {
     __shared__ uint32_t h[kPasses][256];
+    __shared__ unsigned long long sh_groups[2 * kKeyGroups];
     const int g = blockIdx.x * kSortThreads + threadIdx.x;
     if (g < nslot) gal_box[g] = gal_cube(box_bits, g);
     if ((int)blockIdx.x >= ntiles) return;   // blocks past the keys only write galaxy cubes (block-uniform)
     for (int i = threadIdx.x; i < kPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
+    if (threadIdx.x < 2 * kKeyGroups) sh_groups[threadIdx.x] = 0ull;
     zero_tile_status(sort_status, ntiles, pos_status);
     __syncthreads();
     for (int it = 0; it < kSortItems; ++it) {
@@ -777,8 +832,9 @@ __global__ void __launch_bounds__(kSortThreads) k_batch_keys_hist(
         keys[i] = key;
 #pragma unroll
         for (int p = 0; p < kPasses; ++p) atomicAdd(&h[p][(key >> (8 * p)) & 255], 1u);
+        note_group(key, sh_groups);
     }
-    flush_hist(h, ghist);
+    flush_hist(h, sh_groups, ghist);
 }
 
 // --------------------------------------------------------------- host ----
@@ -817,7 +873,7 @@ static cudaError_t reserve_bodies(nb_sim* sim, size_t nk) {
     if (!t.dig_off) NB_TRY(dev_alloc(&t.dig_off, kPasses * 256 * 4));
     if (!t.counters) {
         // counters, tile counters of the look-back kernels, then the radix histograms
-        NB_TRY(dev_alloc(&t.counters, (kCounterWords + kPasses * 256) * 4));
+        NB_TRY(dev_alloc(&t.counters, (kCounterWords + kPasses * 256 + 4 * kKeyGroups) * 4));
         t.ghist = reinterpret_cast<uint32_t*>(t.counters + kCounterWords);
     }
     if (!t.h_counters) NB_TRY(cudaMallocHost(&t.h_counters, TC_COUNT * 4));
@@ -904,7 +960,7 @@ static TopoView topo_view(nb_sim* sim) {
 static cudaError_t launch_keys(nb_sim* sim, size_t nk) {
     TreeBuffers& t = sim->tree;
     const int ntiles = (int)(nk / kSortTile);
-    NB_TRY(cudaMemsetAsync(t.counters, 0, (kCounterWords + kPasses * 256) * 4, sim->stream));
+    NB_TRY(cudaMemsetAsync(t.counters, 0, (kCounterWords + kPasses * 256 + 4 * kKeyGroups) * 4, sim->stream));
     PhaseScope ps(sim, NB_PHASE_KEYS);
     k_keys_hist<<<ntiles, kSortThreads, 0, sim->stream>>>(sim->pos, (int)sim->n, sim->prm.bounds_half,
                                                           sim->prm.max_depth, t.keys[0], t.vals[0], t.depth,
@@ -1023,7 +1079,7 @@ cudaError_t tree_keys_export(nb_sim* sim, uint64_t* d_keys, int32_t* d_depth) {
 // ----------------------------------------------------------------------------
 namespace nb {
 
-int tree_counter_words() { return kCounterWords + kPasses * 256; }
+int tree_counter_words() { return kCounterWords + kPasses * 256 + 4 * kKeyGroups; }
 
 cudaError_t tree_batch_keys(nb_sim* sim, const float4* pos, const int32_t* body_slot, int n,
                             const unsigned* box_bits, int nslot, float4* gal_box) {
