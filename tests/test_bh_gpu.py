@@ -97,6 +97,32 @@ def test_tree_bit_exact_and_forces(model, n, seed):
     assert O.rel_l2(F[::5], F64) < REF_ALGO_FP64_TOL
 
 
+@pytest.mark.parametrize("spread_second", [1.0, 1500.0])
+def test_tree_when_root_octants_fix_the_upper_digits(spread_second):
+    """The radix sort skips a pass whose digit is fixed within each root
+    octant (the top pass orders the octants).  Two clusters in opposite root
+    octants: both tight (levels 2-7 fixed in each octant, passes skipped), or
+    the second spread over its octant (those passes must run); bodies outside
+    the root form their own group.  The tree stays the oracle's either way."""
+    rng = np.random.default_rng(7)
+    a = rng.normal(20.0, 1.0, (3000, 3))
+    b = rng.normal(-20.0, 1.0, (3000, 3)) if spread_second < 10 else -rng.uniform(1.0, spread_second, (3000, 3))
+    out = np.array([[5000.0, 1.0, 1.0], [-4500.0, 0.0, 3.0]])
+    x = np.concatenate([a, b, out]).astype(np.float32)
+    pm = np.concatenate([x, np.full((len(x), 1), 1.0 / len(x), np.float32)], axis=1).astype(np.float32)
+    v = np.zeros_like(pm)
+    rec = nb.records_from_soa(pm, v)
+    t = O.OracleTree(rec)
+    with bh_sim(theta=0.5) as s:
+        s.init(rec)
+        F = s.compute_forces()
+        inter = s.last_interactions()
+        assert_same_tree(s, t)
+    Fo, inter_o = t.forces(G=1.0, S=0.005 ** 2, theta=0.5)
+    assert inter == inter_o
+    assert O.rel_l2(F, Fo) < 1e-5
+
+
 @pytest.mark.parametrize("theta", [0.0, 0.3, 0.6, 1.0, 2.0])
 def test_theta_semantics(theta):
     """theta=0 is direct summation; theta=0.6 lets a body accept its own cell."""
