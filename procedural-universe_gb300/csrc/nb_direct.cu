@@ -176,17 +176,43 @@ __device__ __forceinline__ void write_vertex(nb_render_vertex* rv, const float4*
     o[1] = make_float4(c.y, c.z, c.w, rscale);
 }
 
-__global__ void k_direct_reduce_update(const float4* __restrict__ part, int splits, int n, int n_pad, float G,
-                                       const float4* __restrict__ finit, float4* __restrict__ acc,
-                                       float4* __restrict__ pos, float4* __restrict__ posc,
-                                       float4* __restrict__ vel, float4* __restrict__ velc, float dt,
-                                       float inv_scale, int update, int comp, nb_render_vertex* __restrict__ rv,
-                                       const float4* __restrict__ rcol, float rscale,
-                                       const int* __restrict__ err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || *err != 0) return;
+// Body i's force from its source-split partials ([split][n_pad] sums, then
+// [split][n_pad] compensations): compensated sum of the sums in split order,
+// less the compensations.  The partials of 16 splits are loaded before they
+// are added (in the same order), so that their loads overlap.
+__device__ __forceinline__ float3 fold_partials(const float4* __restrict__ part, int splits, int n_pad, int i) {
     float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-    for (int s = 0; s < splits; ++s) {
+    auto add = [&](const float4 p, const float4 c) {
+        kahan_add(ax, kx, p.x);
+        kahan_add(ay, ky, p.y);
+        kahan_add(az, kz, p.z);
+        qx += c.x; qy += c.y; qz += c.z;
+    };
+    constexpr int kBatch = 16;
+    int s = 0;
+    for (; s + kBatch <= splits; s += kBatch) {
+        float4 p[kBatch], c[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            p[u] = part[(size_t)(s + u) * n_pad + i];
+            c[u] = part[(size_t)(splits + s + u) * n_pad + i];
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) add(p[u], c[u]);
+    }
+    for (; s < splits; ++s) add(part[(size_t)s * n_pad + i], part[(size_t)(splits + s) * n_pad + i]);
+    return make_float3(ax - (kx + qx), ay - (ky + qy), az - (kz + qz));
+}
+
+// kFoldLanes consecutive threads fold one body's partials: lane j takes
+// splits j, j + kFoldLanes, ... (compensated, in that order), and the lanes'
+// corrected sums are added by a butterfly (every lane gets the same total).
+constexpr int kFoldLanes = 8;
+
+__device__ __forceinline__ float3 fold_partials_lanes(const float4* __restrict__ part, int splits, int n_pad, int i,
+                                                      int j) {
+    float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+    for (int s = j; s < splits; s += kFoldLanes) {
         const float4 p = part[(size_t)s * n_pad + i];
         const float4 c = part[(size_t)(splits + s) * n_pad + i];
         kahan_add(ax, kx, p.x);
@@ -194,7 +220,30 @@ __global__ void k_direct_reduce_update(const float4* __restrict__ part, int spli
         kahan_add(az, kz, p.z);
         qx += c.x; qy += c.y; qz += c.z;
     }
-    float3 a = make_float3(G * (ax - (kx + qx)), G * (ay - (ky + qy)), G * (az - (kz + qz)));
+    float3 f = make_float3(ax - (kx + qx), ay - (ky + qy), az - (kz + qz));
+#pragma unroll
+    for (int o = 1; o < kFoldLanes; o <<= 1) {
+        f.x += __shfl_xor_sync(0xffffffffu, f.x, o);
+        f.y += __shfl_xor_sync(0xffffffffu, f.y, o);
+        f.z += __shfl_xor_sync(0xffffffffu, f.z, o);
+    }
+    return f;
+}
+
+__global__ void k_direct_reduce_update(const float4* __restrict__ part, int splits, int n, int n_pad, float G,
+                                       const float4* __restrict__ finit, float4* __restrict__ acc,
+                                       float4* __restrict__ pos, float4* __restrict__ posc,
+                                       float4* __restrict__ vel, float4* __restrict__ velc, float dt,
+                                       float inv_scale, int update, int comp, nb_render_vertex* __restrict__ rv,
+                                       const float4* __restrict__ rcol, float rscale,
+                                       const int* __restrict__ err) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / kFoldLanes, j = t % kFoldLanes;
+    // whole groups of lanes leave together (n_pad bodies, a multiple of the block)
+    if (i >= n_pad || *err != 0) return;
+    const float3 f = fold_partials_lanes(part, splits, n_pad, i, j);
+    if (i >= n || j != 0) return;
+    float3 a = make_float3(G * f.x, G * f.y, G * f.z);
     if (finit) {
         const float4 f = finit[i];
         a.x += f.x; a.y += f.y; a.z += f.z;
@@ -359,7 +408,8 @@ cudaError_t direct_force_update(nb_sim* sim, float dt, bool update) {
     const int n = (int)sim->n;
     const float inv_scale = (float)(1.0 / sim->prm.pos_scale);
     PhaseScope ps(sim, 1);
-    k_direct_reduce_update<<<(n + 255) / 256, 256, 0, sim->stream>>>(
+    static_assert(kPad % (256 / kFoldLanes) == 0, "the fold's blocks cover whole padded bodies");
+    k_direct_reduce_update<<<(unsigned)(sim->n_pad * kFoldLanes / 256), 256, 0, sim->stream>>>(
         sim->part, splits, n, (int)sim->n_pad, (float)sim->prm.G, sim->finit_pending ? sim->finit : nullptr,
         sim->acc, sim->pos, sim->posc, sim->vel, sim->velc, dt, inv_scale, update ? 1 : 0, comp ? 1 : 0,
         update ? sim->render : nullptr, sim->rcolour, sim->rscale, sim->d_err);
@@ -425,16 +475,8 @@ __global__ void k_noalloc_reduce(const float4* __restrict__ part, int splits, in
                                  float4* __restrict__ acc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float ax = 0.f, ay = 0.f, az = 0.f, kx = 0.f, ky = 0.f, kz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-    for (int s = 0; s < splits; ++s) {
-        const float4 p = part[(size_t)s * n_pad + i];
-        const float4 c = part[(size_t)(splits + s) * n_pad + i];
-        kahan_add(ax, kx, p.x);
-        kahan_add(ay, ky, p.y);
-        kahan_add(az, kz, p.z);
-        qx += c.x; qy += c.y; qz += c.z;
-    }
-    float4 a = make_float4(G * (ax - (kx + qx)), G * (ay - (ky + qy)), G * (az - (kz + qz)), 0.f);
+    const float3 f = fold_partials(part, splits, n_pad, i);
+    float4 a = make_float4(G * f.x, G * f.y, G * f.z, 0.f);
     if (g_noalloc_err != 0) a = make_float4(NAN, NAN, NAN, NAN);
     acc[i] = a;
     if (i == 0) g_noalloc_mmax = 0u;
